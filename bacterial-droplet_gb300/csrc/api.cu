@@ -1,0 +1,683 @@
+// api.cu — libttsh host runtime and C ABI (declared in include/ttsh.h).
+//
+// Device memory: one arena per droplet holding its unpadded N^3 fields
+// (phi x2, P, u, u* x2, P* x2, the packed complex Poisson field, and in the plain
+// form the mu_0, mu_b, sigma_ab intermediates) plus its small tables (twiddles,
+// wavenumbers). Droplets of equal N form a group; every kernel of the step is
+// launched once per group, covering all droplets of the group. The whole step
+// (all groups) is captured into a CUDA graph per parity of the ping-pong buffers.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "../../include/ttsh.h"
+#include "common.cuh"
+#include "internal.h"
+#include "kernels.h"
+
+namespace ttsh {
+
+static thread_local std::string g_last_error;
+
+int set_error(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+struct CudaError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+#define CK(call)                                                                                     \
+  do {                                                                                               \
+    cudaError_t e_ = (call);                                                                         \
+    if (e_ != cudaSuccess)                                                                           \
+      throw CudaError(std::string(#call) + ": " + cudaGetErrorString(e_));                          \
+  } while (0)
+
+namespace {
+
+const double kPi = 3.1415926535897932384626433832795;  // TTSH3D.cu:27
+
+std::vector<int> radix_plan(int N) {
+  std::vector<int> r;
+  int m = N;
+  while (m % 4 == 0) { r.push_back(4); m /= 4; }
+  while (m % 2 == 0) { r.push_back(2); m /= 2; }
+  while (m % 3 == 0) { r.push_back(3); m /= 3; }
+  while (m % 5 == 0) { r.push_back(5); m /= 5; }
+  if (m != 1) r.clear();
+  return r;
+}
+
+// Kernel classes reported by ttsh_profile_kernels.
+enum KClass { K_STAGE1, K_STAGE2, K_DIV, K_FFT0, K_FFT1, K_FFT2, K_FFT3, K_FFT4, K_CORRECT, K_FUSED_RHS,
+              K_FUSED_CORRECT, K_NCLASS };
+const char* kNames[K_NCLASS] = {"stage1", "stage2", "div", "fft_x_fwd", "fft_y_fwd", "fft_z_poisson", "fft_y_inv",
+                                "fft_x_inv", "correct", "fused_rhs", "fused_correct"};
+
+struct Prof {
+  cudaStream_t st;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev;
+  void begin(int cls) {
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    CK(cudaEventRecord(a, st));
+    ev.push_back({cls, {a, b}});
+  }
+  void end() { CK(cudaEventRecord(ev.back().second.second, st)); }
+};
+
+struct InstHost {
+  int N = 0;
+  ttsh_input in{};
+  ttsh_ext ext{};
+  double T = 0;
+  void* arena = nullptr;
+};
+
+template <class T>
+struct Engine {
+  std::vector<InstDev<T>> h;     // host copies of the device descriptors
+  std::vector<Group<T>> groups;  // device descriptor arrays
+  std::vector<int> grp, loc;     // instance -> group, index in group
+  std::vector<std::vector<int>> members;
+
+  void free_all() {
+    for (auto& g : groups)
+      if (g.d_inst) cudaFree(g.d_inst);
+    groups.clear();
+  }
+
+  void enqueue_step(int par, cudaStream_t st, bool fused, Prof* pr) {
+    for (auto& g : groups) {
+      auto run = [&](int cls, auto&& fn) {
+        if (pr) pr->begin(cls);
+        fn();
+        if (pr) pr->end();
+      };
+      if (fused) {
+        run(K_FUSED_RHS, [&] { launch_fused_rhs_t(g, par, st); });
+      } else {
+        run(K_STAGE1, [&] { launch_stage1<T>(g, par, st); });
+        run(K_STAGE2, [&] { launch_stage2<T>(g, par, st); });
+        run(K_DIV, [&] { launch_div<T>(g, par, st); });
+      }
+      for (int pass = 0; pass < 5; ++pass) run(K_FFT0 + pass, [&] { launch_fft_pass<T>(g, pass, st); });
+      if (fused) run(K_FUSED_CORRECT, [&] { launch_fused_correct_t(g, par, st); });
+      else run(K_CORRECT, [&] { launch_correct<T>(g, par, st); });
+    }
+  }
+  void launch_fused_rhs_t(const Group<T>& g, int par, cudaStream_t st);
+  void launch_fused_correct_t(const Group<T>& g, int par, cudaStream_t st);
+  int launches(bool fused) const { return (int)groups.size() * (fused ? 7 : 9); }
+};
+
+template <>
+void Engine<float>::launch_fused_rhs_t(const Group<float>& g, int par, cudaStream_t st) { launch_fused_rhs(g, par, st); }
+template <>
+void Engine<float>::launch_fused_correct_t(const Group<float>& g, int par, cudaStream_t st) {
+  launch_fused_correct(g, par, st);
+}
+template <>
+void Engine<double>::launch_fused_rhs_t(const Group<double>&, int, cudaStream_t) {
+  throw std::runtime_error("fused form is FP32 only");
+}
+template <>
+void Engine<double>::launch_fused_correct_t(const Group<double>&, int, cudaStream_t) {
+  throw std::runtime_error("fused form is FP32 only");
+}
+
+}  // namespace
+}  // namespace ttsh
+
+using namespace ttsh;
+
+struct ttsh_sim {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int precision = 64;
+  bool fused = false;
+  std::vector<InstHost> inst;
+  Engine<float> ef;
+  Engine<double> ed;
+  int par = 0;
+  int64_t steps = 0;
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  std::vector<void*> tables;  // shared per-N tables
+
+  template <class F>
+  void with_engine(F&& f) {
+    if (precision == 32) f(ef);
+    else f(ed);
+  }
+};
+
+namespace {
+
+// Validation of one droplet's parameters; returns 0 or sets the error.
+int validate(const ttsh_input& in, const ttsh_ext& ext) {
+  if (in.ReadSuccess != TTSH_READ_SUCCESS) return set_error(TTSH_E_PARSE, "input: ReadSuccess != -8848");
+  if (in.Nx != in.Ny || in.Ny != in.Nz)
+    return set_error(TTSH_E_UNSUPPORTED, "grid must be cubic (the reference's FFT plan, TTSH3D.cu:1123)");
+  if (in.Nx < 8 || in.Nx > 1024) return set_error(TTSH_E_UNSUPPORTED, "N must be in [8, 1024]");
+  if (radix_plan(in.Nx).empty()) return set_error(TTSH_E_UNSUPPORTED, "N must factor into 2, 3, 5");
+  if (!(in.h > 0) || !(in.dt0 > 0)) return set_error(TTSH_E_INVALID, "h and dt0 must be > 0");
+  if (in.TimeScheme != 1)
+    return set_error(TTSH_E_UNSUPPORTED, "only TimeScheme 1 (explicit Euler) exists in the reference step");
+  if (ext.precision != 32 && ext.precision != 64) return set_error(TTSH_E_INVALID, "precision must be 32 or 64");
+  if (ext.k2_mode != 0 && ext.k2_mode != 1) return set_error(TTSH_E_INVALID, "k2_mode must be 0 or 1");
+  return TTSH_OK;
+}
+
+template <class T>
+Phys<T> make_phys(const ttsh_input& in, const ttsh_ext& ext) {
+  Phys<T> p{};
+  const double h = in.h;
+  p.h = (T)h;
+  p.dt = (T)in.dt0;
+  p.inv_dt = (T)(1.0 / in.dt0);
+  p.dt_d = in.dt0;
+  p.mu = (T)in.mu; p.cA = (T)in.cA; p.alpha = (T)in.alpha; p.beta = (T)in.beta; p.eta = (T)in.eta;
+  p.La2 = (T)(in.La * in.La);
+  p.kappa = (T)in.kappa; p.lambda0 = (T)in.lambda0;
+  p.aPhi2 = (T)(in.aPhi * 2);
+  p.kPhi = (T)in.kPhi; p.gamma = (T)in.gamma; p.A = (T)in.A; p.zeta = (T)ext.zeta;
+  p.c2h = (T)(1.0 / (2.0 * h));
+  p.cl12 = (T)(1.0 / (12 * h * h));
+  p.cl23 = (T)(2.0 / (3 * h * h));
+  p.cl143 = (T)(14.0 / (3 * h * h));
+  const double n3 = (double)in.Nx * in.Nx * in.Nx;
+  p.invN3 = (T)(1.0 / n3);
+  return p;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+template <class T>
+void build_engine(ttsh_sim* s, Engine<T>& E) {
+  typedef typename CxT<T>::type C;
+  const int n = (int)s->inst.size();
+  E.h.resize(n);
+  E.grp.resize(n);
+  E.loc.resize(n);
+  std::map<int, int> by_n;
+  for (int i = 0; i < n; ++i) {
+    const int N = s->inst[i].N;
+    if (!by_n.count(N)) {
+      by_n[N] = (int)E.members.size();
+      E.members.push_back({});
+    }
+    E.grp[i] = by_n[N];
+    E.loc[i] = (int)E.members[E.grp[i]].size();
+    E.members[E.grp[i]].push_back(i);
+  }
+  // per-N tables
+  std::map<int, InstDev<T>> tab;
+  for (auto& kv : by_n) {
+    const int N = kv.first;
+    const double h = s->inst[E.members[kv.second][0]].in.h;
+    std::vector<C> tw(N);
+    std::vector<double> kval(N);
+    std::vector<T> k2t(N), St(N), Ct(N);
+    for (int k = 0; k < N; ++k) {
+      const double a = -2.0 * kPi * (double)k / (double)N;
+      tw[k].x = (T)std::cos(a);
+      tw[k].y = (T)std::sin(a);
+      // initPoissonSolver (TTSH3D.cu:1093-1117)
+      double kk = 2 * kPi * k / (N * h + 0.0);
+      if (k >= N / 2) kk = 2 * kPi * (k - N) / (N * h + 0.0);
+      kval[k] = kk;
+      k2t[k] = (T)(kk * kk);
+      St[k] = (T)(std::sin(kk * h) / h);
+      Ct[k] = (T)((2.0 + std::cos(kk * h)) / 3.0);
+    }
+    size_t bytes = align256(N * sizeof(C)) + align256(N * sizeof(double)) + 3 * align256(N * sizeof(T));
+    char* d = nullptr;
+    CK(cudaMalloc(&d, bytes));
+    s->tables.push_back(d);
+    InstDev<T> t{};
+    size_t off = 0;
+    t.tw = reinterpret_cast<C*>(d + off); CK(cudaMemcpy(d + off, tw.data(), N * sizeof(C), cudaMemcpyHostToDevice));
+    off += align256(N * sizeof(C));
+    t.kval = reinterpret_cast<double*>(d + off);
+    CK(cudaMemcpy(d + off, kval.data(), N * sizeof(double), cudaMemcpyHostToDevice));
+    off += align256(N * sizeof(double));
+    t.k2t = reinterpret_cast<T*>(d + off); CK(cudaMemcpy(d + off, k2t.data(), N * sizeof(T), cudaMemcpyHostToDevice));
+    off += align256(N * sizeof(T));
+    t.St = reinterpret_cast<T*>(d + off); CK(cudaMemcpy(d + off, St.data(), N * sizeof(T), cudaMemcpyHostToDevice));
+    off += align256(N * sizeof(T));
+    t.Ct = reinterpret_cast<T*>(d + off); CK(cudaMemcpy(d + off, Ct.data(), N * sizeof(T), cudaMemcpyHostToDevice));
+    tab[N] = t;
+    fft_prepare<T>(N);
+  }
+  // per-instance arenas
+  for (int i = 0; i < n; ++i) {
+    InstHost& ih = s->inst[i];
+    const int N = ih.N;
+    const size_t nn = (size_t)N * N * N;
+    const size_t fb = align256(nn * sizeof(T));
+    const int nfields = 2 + 3 + 3 + 6 + 6 + (s->fused ? 0 : 13);
+    const size_t red_bytes = align256(4 * sizeof(double) * (size_t)stats_partials_per_instance(N));
+    const size_t bytes = nfields * fb + align256(nn * sizeof(C)) + red_bytes;
+    char* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, bytes);
+    if (e != cudaSuccess) throw std::bad_alloc();
+    ih.arena = d;
+    CK(cudaMemset(d, 0, bytes));
+    InstDev<T>& I = E.h[i];
+    I = tab[N];
+    I.N = N;
+    I.stale = (ih.ext.quirks & TTSH_QUIRK_STALE_HALO) ? 1 : 0;
+    I.k2mode = ih.ext.k2_mode;
+    std::vector<int> r = radix_plan(N);
+    I.nstages = (int)r.size();
+    for (size_t k = 0; k < r.size(); ++k) I.radix[k] = r[k];
+    I.ph = make_phys<T>(ih.in, ih.ext);
+    size_t off = 0;
+    auto take = [&]() { T* p = reinterpret_cast<T*>(d + off); off += fb; return p; };
+    I.phi[0] = take(); I.phi[1] = take();
+    for (int b = 0; b < 3; ++b) I.P[b] = take();
+    for (int b = 0; b < 3; ++b) I.U[b] = take();
+    for (int q = 0; q < 2; ++q)
+      for (int b = 0; b < 3; ++b) I.Us[q][b] = take();
+    for (int q = 0; q < 2; ++q)
+      for (int b = 0; b < 3; ++b) I.Ps[q][b] = take();
+    if (!s->fused) {
+      I.mu0 = take();
+      for (int b = 0; b < 3; ++b) I.mu[b] = take();
+      for (int b = 0; b < 9; ++b) I.sig[b] = take();
+    }
+    I.W = reinterpret_cast<C*>(d + off);
+    off += align256(nn * sizeof(C));
+    I.red = reinterpret_cast<double*>(d + off);
+  }
+  for (size_t g = 0; g < E.members.size(); ++g) {
+    Group<T> G{};
+    G.n = (int)E.members[g].size();
+    G.N = s->inst[E.members[g][0]].N;
+    std::vector<InstDev<T>> arr;
+    for (int i : E.members[g]) arr.push_back(E.h[i]);
+    CK(cudaMalloc(&G.d_inst, sizeof(InstDev<T>) * arr.size()));
+    CK(cudaMemcpy(G.d_inst, arr.data(), sizeof(InstDev<T>) * arr.size(), cudaMemcpyHostToDevice));
+    E.groups.push_back(G);
+  }
+  // the arena memsets ran on the legacy stream, which the non-blocking step stream does not wait for
+  CK(cudaDeviceSynchronize());
+}
+
+void capture_graphs(ttsh_sim* s) {
+  for (int q = 0; q < 2; ++q) {
+    if (s->gexec[q]) { cudaGraphExecDestroy(s->gexec[q]); s->gexec[q] = nullptr; }
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeRelaxed));
+    try {
+      s->with_engine([&](auto& E) { E.enqueue_step(q, s->stream, s->fused, nullptr); });
+    } catch (...) {
+      cudaStreamEndCapture(s->stream, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    CK(cudaStreamEndCapture(s->stream, &g));
+    CK(cudaGraphInstantiate(&s->gexec[q], g, 0));
+    CK(cudaGraphDestroy(g));
+  }
+}
+
+void release(ttsh_sim* s) {
+  if (!s) return;
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (int q = 0; q < 2; ++q)
+    if (s->gexec[q]) cudaGraphExecDestroy(s->gexec[q]);
+  s->ef.free_all();
+  s->ed.free_all();
+  for (auto& ih : s->inst)
+    if (ih.arena) cudaFree(ih.arena);
+  for (void* p : s->tables) cudaFree(p);
+  if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+}
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    return f();
+  } catch (const CudaError& e) {
+    return set_error(TTSH_E_CUDA, e.what());
+  } catch (const std::bad_alloc&) {
+    return set_error(TTSH_E_NOMEM, "allocation failed");
+  } catch (const std::exception& e) {
+    return set_error(TTSH_E_CUDA, e.what());
+  }
+}
+
+bool fused_ok(const ttsh_sim* s) {
+  if (s->precision != 32) return false;
+  for (auto& ih : s->inst)
+    if (!fused_supported(ih.N)) return false;
+  return true;
+}
+
+}  // namespace
+
+// Host (FP64) <-> device (T) copies of one N^3 field.
+template <class T>
+static void h2d(T* dst, const double* src, size_t n, cudaStream_t st) {
+  if (sizeof(T) == sizeof(double)) {
+    CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+  } else {
+    std::vector<T> tmp(n);
+    for (size_t i = 0; i < n; ++i) tmp[i] = (T)src[i];
+    CK(cudaMemcpyAsync(dst, tmp.data(), n * sizeof(T), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+  }
+}
+template <class T>
+static void d2h(double* dst, const T* src, size_t n, cudaStream_t st, size_t stride = 1) {
+  if (sizeof(T) == sizeof(double) && stride == 1) {
+    CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+  } else {
+    std::vector<T> tmp(n * stride);
+    CK(cudaMemcpyAsync(tmp.data(), src, n * stride * sizeof(T), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (size_t i = 0; i < n; ++i) dst[i] = (double)tmp[i * stride];
+  }
+}
+
+extern "C" {
+
+int ttsh_batch_create(const ttsh_input* in, const ttsh_ext* ext, int n, int device, ttsh_sim** out) {
+  if (!in || !out || n <= 0) return set_error(TTSH_E_INVALID, "ttsh_batch_create: bad arguments");
+  *out = nullptr;
+  ttsh_ext dflt;
+  ttsh_default_ext(&dflt);
+  for (int i = 0; i < n; ++i) {
+    int rc = validate(in[i], ext ? ext[i] : dflt);
+    if (rc) return rc;
+    if ((ext ? ext[i].precision : dflt.precision) != (ext ? ext[0].precision : dflt.precision))
+      return set_error(TTSH_E_INVALID, "all instances of a batch share one precision");
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return set_error(TTSH_E_NODEVICE, "no CUDA device visible (check CUDA_VISIBLE_DEVICES)");
+  }
+  ttsh_sim* s = new ttsh_sim();
+  return guarded([&]() -> int {
+    try {
+      if (device < 0) CK(cudaGetDevice(&device));
+      if (device >= ndev) throw std::runtime_error("device index out of range");
+      s->device = device;
+      CK(cudaSetDevice(device));
+      CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+      s->own_stream = true;
+      s->precision = ext ? ext[0].precision : dflt.precision;
+      s->inst.resize(n);
+      for (int i = 0; i < n; ++i) {
+        s->inst[i].in = in[i];
+        s->inst[i].ext = ext ? ext[i] : dflt;
+        s->inst[i].N = in[i].Nx;
+        s->inst[i].T = in[i].T0;
+      }
+      s->fused = fused_ok(s);
+      if (s->precision == 32) build_engine<float>(s, s->ef);
+      else build_engine<double>(s, s->ed);
+      capture_graphs(s);
+      CK(cudaStreamSynchronize(s->stream));
+      *out = s;
+      return TTSH_OK;
+    } catch (...) {
+      release(s);
+      throw;
+    }
+  });
+}
+
+int ttsh_create(const ttsh_input* in, const ttsh_ext* ext, int device, ttsh_sim** out) {
+  return ttsh_batch_create(in, ext, 1, device, out);
+}
+
+int ttsh_set_stream(ttsh_sim* s, void* stream) {
+  if (!s) return set_error(TTSH_E_INVALID, "null handle");
+  return guarded([&]() -> int {
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    if (stream) {
+      if (s->own_stream) CK(cudaStreamDestroy(s->stream));
+      s->own_stream = false;
+      s->stream = (cudaStream_t)stream;
+    } else if (!s->own_stream) {
+      CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+      s->own_stream = true;
+    }
+    return TTSH_OK;
+  });
+}
+
+void ttsh_destroy(ttsh_sim* s) { release(s); }
+
+int ttsh_num_instances(const ttsh_sim* s) { return s ? (int)s->inst.size() : 0; }
+int ttsh_instance_n(const ttsh_sim* s, int inst) {
+  return (s && inst >= 0 && inst < (int)s->inst.size()) ? s->inst[inst].N : 0;
+}
+double ttsh_time(const ttsh_sim* s) { return (s && !s->inst.empty()) ? s->inst[0].T : 0.0; }
+int ttsh_launches_per_step(const ttsh_sim* s) {
+  if (!s) return 0;
+  return s->precision == 32 ? s->ef.launches(s->fused) : s->ed.launches(s->fused);
+}
+
+static int check_inst(ttsh_sim* s, int inst) {
+  if (!s) return set_error(TTSH_E_INVALID, "null handle");
+  if (inst < 0 || inst >= (int)s->inst.size()) return set_error(TTSH_E_INVALID, "instance index out of range");
+  return TTSH_OK;
+}
+
+int ttsh_set_state(ttsh_sim* s, int inst, const double* phi, const double* P, const double* u, const double* ustar,
+                   const double* Pstar) {
+  int rc = check_inst(s, inst);
+  if (rc) return rc;
+  if (!phi || !P || !u) return set_error(TTSH_E_INVALID, "phi, P and u are required");
+  return guarded([&]() -> int {
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    const int N = s->inst[inst].N;
+    const size_t n = (size_t)N * N * N;
+    s->with_engine([&](auto& E) {
+      auto& I = E.h[inst];
+      typedef typename std::decay<decltype(*I.phi[0])>::type TT;
+      h2d<TT>(I.phi[s->par], phi, n, s->stream);
+      for (int b = 0; b < 3; ++b) {
+        h2d<TT>(I.P[b], P + b * n, n, s->stream);
+        h2d<TT>(I.U[b], u + b * n, n, s->stream);
+        if (ustar) h2d<TT>(I.Us[s->par][b], ustar + b * n, n, s->stream);
+        else CK(cudaMemsetAsync(I.Us[s->par][b], 0, n * sizeof(TT), s->stream));
+        if (Pstar) h2d<TT>(I.Ps[s->par][b], Pstar + b * n, n, s->stream);
+        else CK(cudaMemsetAsync(I.Ps[s->par][b], 0, n * sizeof(TT), s->stream));
+      }
+      CK(cudaStreamSynchronize(s->stream));
+    });
+    return TTSH_OK;
+  });
+}
+
+int ttsh_step(ttsh_sim* s, int nsteps) {
+  if (!s || nsteps < 0) return set_error(TTSH_E_INVALID, "ttsh_step: bad arguments");
+  return guarded([&]() -> int {
+    CK(cudaSetDevice(s->device));
+    for (int t = 0; t < nsteps; ++t) {
+      CK(cudaGraphLaunch(s->gexec[s->par], s->stream));
+      s->par ^= 1;
+      s->steps += 1;
+      for (auto& ih : s->inst) ih.T = ih.T + ih.in.dt0;  // run(): T = T + Dt (TTSH3D.cu:342)
+    }
+    return TTSH_OK;
+  });
+}
+
+int ttsh_sync(ttsh_sim* s) {
+  if (!s) return set_error(TTSH_E_INVALID, "null handle");
+  return guarded([&]() -> int {
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    return TTSH_OK;
+  });
+}
+
+int ttsh_get_state(ttsh_sim* s, int inst, double* phi, double* P, double* u, double* p_v, double* p_p) {
+  int rc = check_inst(s, inst);
+  if (rc) return rc;
+  return guarded([&]() -> int {
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    const int N = s->inst[inst].N;
+    const size_t n = (size_t)N * N * N;
+    s->with_engine([&](auto& E) {
+      auto& I = E.h[inst];
+      typedef typename std::decay<decltype(*I.phi[0])>::type TT;
+      if (phi) d2h<TT>(phi, I.phi[s->par], n, s->stream);
+      for (int b = 0; b < 3; ++b) {
+        if (P) d2h<TT>(P + b * n, I.P[b], n, s->stream);
+        if (u) d2h<TT>(u + b * n, I.U[b], n, s->stream);
+      }
+      const TT* w = reinterpret_cast<const TT*>(I.W);
+      if (p_v) d2h<TT>(p_v, w, n, s->stream, 2);
+      if (p_p) d2h<TT>(p_p, w + 1, n, s->stream, 2);
+    });
+    return TTSH_OK;
+  });
+}
+
+int ttsh_get_provisional(ttsh_sim* s, int inst, double* ustar, double* Pstar) {
+  int rc = check_inst(s, inst);
+  if (rc) return rc;
+  return guarded([&]() -> int {
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    const int N = s->inst[inst].N;
+    const size_t n = (size_t)N * N * N;
+    s->with_engine([&](auto& E) {
+      auto& I = E.h[inst];
+      typedef typename std::decay<decltype(*I.phi[0])>::type TT;
+      for (int b = 0; b < 3; ++b) {
+        if (ustar) d2h<TT>(ustar + b * n, I.Us[s->par][b], n, s->stream);
+        if (Pstar) d2h<TT>(Pstar + b * n, I.Ps[s->par][b], n, s->stream);
+      }
+    });
+    return TTSH_OK;
+  });
+}
+
+int ttsh_reduce(ttsh_sim* s, int inst, ttsh_stats* out) {
+  int rc = check_inst(s, inst);
+  if (rc) return rc;
+  if (!out) return set_error(TTSH_E_INVALID, "null stats");
+  return guarded([&]() -> int {
+    CK(cudaSetDevice(s->device));
+    const InstHost& ih = s->inst[inst];
+    std::vector<double> part;
+    s->with_engine([&](auto& E) {
+      const int g = E.grp[inst];
+      const int nb = launch_stats(E.groups[g], s->par, s->stream);
+      part.resize(4 * (size_t)nb);
+      CK(cudaMemcpyAsync(part.data(), E.h[inst].red, part.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                         s->stream));
+      CK(cudaStreamSynchronize(s->stream));
+    });
+    double sum = 0, md = 0, mu = 0, bad = 0;
+    for (size_t b = 0; b < part.size() / 4; ++b) {
+      sum += part[4 * b];
+      md = std::max(md, part[4 * b + 1]);
+      mu = std::max(mu, part[4 * b + 2]);
+      bad += part[4 * b + 3];
+    }
+    const double h = ih.in.h;
+    out->mass = sum * h * h * h;
+    out->max_div_u = md;
+    out->max_abs_u = mu;
+    out->T = ih.T;
+    out->steps = s->steps;
+    out->nonfinite = bad > 0 ? 1 : 0;
+    out->reserved = 0;
+    return bad > 0 ? set_error(TTSH_E_UNSTABLE, "non-finite values in the state") : TTSH_OK;
+  });
+}
+
+int ttsh_write_conf(ttsh_sim* s, int inst, const char* path) {
+  int rc = check_inst(s, inst);
+  if (rc) return rc;
+  const int N = s->inst[inst].N;
+  const size_t n = (size_t)N * N * N;
+  std::vector<double> phi(n), P(3 * n), u(3 * n);
+  rc = ttsh_get_state(s, inst, phi.data(), P.data(), u.data(), nullptr, nullptr);
+  if (rc) return rc;
+  return ttsh_format_conf(N, s->inst[inst].in.ExpoData, phi.data(), P.data(), u.data(), path);
+}
+
+int ttsh_profile_kernels(ttsh_sim* s, int nsteps, int cap, const char** names, double* ms_per_step,
+                         int64_t* launches_per_step) {
+  if (!s || nsteps <= 0 || cap <= 0 || !names || !ms_per_step) return set_error(TTSH_E_INVALID, "bad arguments");
+  int written = 0;
+  int rc = guarded([&]() -> int {
+    CK(cudaSetDevice(s->device));
+    Prof pr;
+    pr.st = s->stream;
+    for (int t = 0; t < nsteps; ++t) {
+      s->with_engine([&](auto& E) { E.enqueue_step(s->par, s->stream, s->fused, &pr); });
+      s->par ^= 1;
+      s->steps += 1;
+      for (auto& ih : s->inst) ih.T = ih.T + ih.in.dt0;
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    std::vector<double> tot(K_NCLASS, 0.0);
+    std::vector<int64_t> cnt(K_NCLASS, 0);
+    for (auto& e : pr.ev) {
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, e.second.first, e.second.second));
+      tot[e.first] += ms;
+      cnt[e.first] += 1;
+      cudaEventDestroy(e.second.first);
+      cudaEventDestroy(e.second.second);
+    }
+    for (int c = 0; c < K_NCLASS && written < cap; ++c) {
+      if (!cnt[c]) continue;
+      names[written] = kNames[c];
+      ms_per_step[written] = tot[c] / nsteps;
+      if (launches_per_step) launches_per_step[written] = cnt[c] / nsteps;
+      ++written;
+    }
+    return TTSH_OK;
+  });
+  return rc ? -rc : written;
+}
+
+const char* ttsh_strerror(int code) {
+  switch (code) {
+    case TTSH_OK: return "ok";
+    case TTSH_E_INVALID: return "invalid argument";
+    case TTSH_E_IO: return "i/o error";
+    case TTSH_E_PARSE: return "Error while reading the input file!";
+    case TTSH_E_CUDA: return "CUDA error";
+    case TTSH_E_NODEVICE: return "no CUDA device";
+    case TTSH_E_NOMEM: return "out of memory";
+    case TTSH_E_UNSTABLE: return "non-finite state";
+    case TTSH_E_UNSUPPORTED: return "unsupported size or option";
+    default: return "unknown error";
+  }
+}
+
+const char* ttsh_last_error(void) { return g_last_error.c_str(); }
+
+}  // extern "C"

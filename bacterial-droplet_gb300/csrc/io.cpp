@@ -1,0 +1,190 @@
+// io.cpp — host-side boundary of libttsh: the input.dat reader, the snapshot
+// writer and the build-defined initial condition. No CUDA here.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/ttsh.h"
+#include "internal.h"
+
+using ttsh::set_error;
+
+extern "C" {
+
+// GetInput (TTSH3D.cu:696-752): the same 33 extractions, in the same order and into
+// the same types, so a file the reference accepts is accepted here and vice versa.
+int ttsh_read_input(const char* path, ttsh_input* o) {
+  if (!path || !o) return set_error(TTSH_E_INVALID, "ttsh_read_input: null argument");
+  std::ifstream f(path);
+  if (!f.is_open()) return set_error(TTSH_E_IO, std::string("cannot open ") + path);
+  std::memset(o, 0, sizeof(*o));
+  o->ReadSuccess = 0;
+  f >> o->TimeScheme >> o->RKStage >> o->ExplImpi >> o->AdapTime >> o->ExpoData >> o->InitCond >> o->isSimplified >>
+      o->checkUnStable;
+  f >> o->Nx >> o->Ny >> o->Nz >> o->Nb;
+  f >> o->h >> o->dt0 >> o->T0 >> o->Ts >> o->dte >> o->dtVarC >> o->dtMax;
+  f >> o->mu >> o->cA >> o->alpha >> o->beta >> o->eta >> o->La >> o->kappa >> o->lambda0 >> o->aPhi >> o->kPhi >>
+      o->gamma >> o->A >> o->init0;
+  f >> o->ReadSuccess;
+  if (o->ReadSuccess != TTSH_READ_SUCCESS)
+    return set_error(TTSH_E_PARSE, "Error while reading the input file!");  // TTSH3D.cu:750
+  return TTSH_OK;
+}
+
+// run_cuda.pl:7-44 (the parameters it writes to input.dat).
+void ttsh_default_input(ttsh_input* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->TimeScheme = 1; o->RKStage = 16; o->ExplImpi = 1; o->AdapTime = 0; o->ExpoData = 1; o->InitCond = 1;
+  o->isSimplified = 1; o->checkUnStable = 0;
+  o->Nx = o->Ny = o->Nz = 64; o->Nb = 3;
+  o->h = 1; o->dt0 = 0.002; o->T0 = 0; o->Ts = 1000; o->dte = 10; o->dtVarC = 0.01; o->dtMax = 0.000005;
+  o->mu = 1; o->cA = -1; o->alpha = -0.02; o->beta = 4.366; o->eta = -0.187; o->La = 1; o->kappa = -0.364;
+  o->lambda0 = 9; o->aPhi = 1; o->kPhi = 1; o->gamma = 1; o->A = 0; o->init0 = 0.0001;
+  o->ReadSuccess = TTSH_READ_SUCCESS;
+}
+
+void ttsh_default_ext(ttsh_ext* e) {
+  if (!e) return;
+  std::memset(e, 0, sizeof(*e));
+  e->zeta = 0; e->R = 16; e->xi = 2; e->seed = 0; e->precision = 64;
+  e->k2_mode = TTSH_K2_REFERENCE; e->quirks = TTSH_QUIRK_STALE_HALO;
+}
+
+// ExpoConf's text layout (TTSH3D.cu:966-1013): y outer, x, z inner; ExpoData == 1 writes
+// "vx vy vz px py pz phi\n" and ExpoData == -1 writes "vx vy " (no newline), each value as
+// `fixed << setprecision(15)`, i.e. printf "%.15f". Lines are formatted in parallel and
+// written in order.
+int ttsh_format_conf(int N, int expo_data, const double* phi, const double* P, const double* u, const char* path) {
+  if (N <= 0 || !path) return set_error(TTSH_E_INVALID, "ttsh_format_conf: bad arguments");
+  if (expo_data == 1 && (!phi || !P || !u)) return set_error(TTSH_E_INVALID, "ttsh_format_conf: null field");
+  if (expo_data == -1 && !u) return set_error(TTSH_E_INVALID, "ttsh_format_conf: null field");
+  FILE* fp = std::fopen(path, "wb");
+  if (!fp) return set_error(TTSH_E_IO, std::string("cannot open ") + path);
+  if (expo_data != 1 && expo_data != -1) {  // the reference's loop writes nothing
+    std::fclose(fp);
+    return TTSH_OK;
+  }
+  const size_t n = (size_t)N * N * N;
+  const size_t NN = (size_t)N * N;
+  unsigned nth = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+  // Each round formats nth chunks of consecutive y-planes (the outer loop) and writes them in
+  // order; a chunk holds about 8 MB of text at most, so memory stays bounded.
+  const int chunk_rows = std::max(1, (int)std::min<size_t>((size_t)N / nth, (size_t)(8u << 20) / (NN * 140)));
+  int err = 0;
+  for (int y0 = 0; y0 < N && !err; y0 += chunk_rows * (int)nth) {
+    std::vector<std::string> bufs(nth);
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nth; ++t) {
+      th.emplace_back([&, t]() {
+        const int ya = y0 + (int)t * chunk_rows;
+        const int yb = std::min(N, ya + chunk_rows);
+        if (ya >= yb) return;
+        std::string& out = bufs[t];
+        out.reserve((size_t)(yb - ya) * NN * (expo_data == 1 ? 7 * 20 : 2 * 20));
+        char tmp[512];
+        for (int y = ya; y < yb; ++y)
+          for (int x = 0; x < N; ++x)
+            for (int z = 0; z < N; ++z) {
+              const size_t i = ((size_t)z * N + y) * N + x;
+              int len;
+              if (expo_data == 1)
+                len = std::snprintf(tmp, sizeof(tmp), "%.15f %.15f %.15f %.15f %.15f %.15f %.15f\n", u[i], u[n + i],
+                                    u[2 * n + i], P[i], P[n + i], P[2 * n + i], phi[i]);
+              else
+                len = std::snprintf(tmp, sizeof(tmp), "%.15f %.15f ", u[i], u[n + i]);
+              out.append(tmp, (size_t)len);
+            }
+      });
+    }
+    for (auto& t : th) t.join();
+    for (auto& b : bufs)
+      if (!b.empty() && std::fwrite(b.data(), 1, b.size(), fp) != b.size()) err = 1;
+  }
+  if (std::fclose(fp) != 0) err = 1;
+  if (err) return set_error(TTSH_E_IO, std::string("write failed: ") + path);
+  return TTSH_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+inline uint64_t splitmix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+// Counter-based uniform in [0,1): stream `k` of site `idx` under `seed`.
+inline double uni(uint64_t seed, uint64_t idx, uint64_t k) {
+  return (double)(splitmix64(splitmix64(seed) ^ (idx * 8 + k)) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+}  // namespace
+
+extern "C" int ttsh_init_droplet(int N, double h, double R, double xi, uint64_t seed, double angular_noise, double* phi,
+                                 double* P) {
+  if (N < 4 || !(h > 0) || !(xi > 0) || !phi || !P)
+    return set_error(TTSH_E_INVALID, "ttsh_init_droplet: bad arguments");
+  const size_t n = (size_t)N * N * N;
+  const double c = N / 2.0, twopi = 6.283185307179586476925286766559;
+  std::vector<double> Q(3 * n, 0.0);
+  for (int z = 0; z < N; ++z)
+    for (int y = 0; y < N; ++y)
+      for (int x = 0; x < N; ++x) {
+        const size_t i = ((size_t)z * N + y) * N + x;
+        const double dx = x - c, dy = y - c, dz = z - c;
+        const double r = h * std::sqrt(dx * dx + dy * dy + dz * dz);
+        phi[i] = 0.5 * (1.0 - std::tanh((r - R) / xi));
+        if (phi[i] > 0.5) {
+          const double cz = 1.0 - 2.0 * uni(seed, i, 0);
+          const double az = twopi * uni(seed, i, 1);
+          const double s = std::sqrt(std::max(0.0, 1.0 - cz * cz));
+          double v[3] = {s * std::cos(az), s * std::sin(az), cz};
+          if (angular_noise > 0) {
+            double g[3];
+            for (int k = 0; k < 3; ++k) {  // Box-Muller
+              const double u1 = 1.0 - uni(seed, i, 2 + k), u2 = uni(seed, i, 5 + (k % 3));
+              g[k] = std::sqrt(-2.0 * std::log(u1)) * std::cos(twopi * u2);
+            }
+            const double gp = g[0] * v[0] + g[1] * v[1] + g[2] * v[2];
+            double w[3], nn = 0;
+            for (int k = 0; k < 3; ++k) {
+              w[k] = v[k] + angular_noise * (g[k] - gp * v[k]);
+              nn += w[k] * w[k];
+            }
+            nn = std::sqrt(nn);
+            for (int k = 0; k < 3; ++k) v[k] = w[k] / nn;
+          }
+          for (int k = 0; k < 3; ++k) Q[k * n + i] = v[k];
+        }
+      }
+  // 3 Jacobi passes: mean of self and the 6 face neighbours, periodic.
+  std::vector<double> T2(3 * n);
+  for (int pass = 0; pass < 3; ++pass) {
+    for (int k = 0; k < 3; ++k) {
+      const double* a = &Q[k * n];
+      double* b = &T2[k * n];
+      for (int z = 0; z < N; ++z)
+        for (int y = 0; y < N; ++y)
+          for (int x = 0; x < N; ++x) {
+            auto at = [&](int X, int Y, int Z) {
+              X = (X + N) % N; Y = (Y + N) % N; Z = (Z + N) % N;
+              return a[((size_t)Z * N + Y) * N + X];
+            };
+            b[((size_t)z * N + y) * N + x] = (at(x, y, z) + at(x - 1, y, z) + at(x + 1, y, z) + at(x, y - 1, z) +
+                                              at(x, y + 1, z) + at(x, y, z - 1) + at(x, y, z + 1)) / 7.0;
+          }
+    }
+    Q.swap(T2);
+  }
+  for (size_t i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) P[k * n + i] = phi[i] > 0.5 ? Q[k * n + i] : 0.0;
+  return TTSH_OK;
+}

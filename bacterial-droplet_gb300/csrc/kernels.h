@@ -1,0 +1,38 @@
+// kernels.h — host-side launch interface of libttsh's CUDA kernels (no device code here).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace ttsh {
+
+template <class T> struct InstDev;
+
+// One group = instances of equal N sharing a device array of descriptors.
+template <class T>
+struct Group {
+  InstDev<T>* d_inst;  // device array [n]
+  int n;               // instances in the group
+  int N;
+};
+
+// Plain form (one thread per site, reference arithmetic order), plain.cu.
+template <class T> void launch_stage1(const Group<T>& g, int par, cudaStream_t st);
+template <class T> void launch_stage2(const Group<T>& g, int par, cudaStream_t st);
+template <class T> void launch_div(const Group<T>& g, int par, cudaStream_t st);
+template <class T> void launch_correct(const Group<T>& g, int par, cudaStream_t st);
+// FP64 diagnostics: per-instance partials into d_inst[i].red (nblocks_out per instance).
+template <class T> int launch_stats(const Group<T>& g, int par, cudaStream_t st);
+int stats_partials_per_instance(int N);
+
+// Poisson solve by FFT (fft.cu): W <- (inverse FFT of -FFT(W)/k^2) / N^3.
+// pass 0: forward x; 1: forward y; 2: forward z, divide, inverse z; 3: inverse y; 4: inverse x + scale.
+template <class T> void launch_fft_pass(const Group<T>& g, int pass, cudaStream_t st);
+template <class T> size_t fft_smem_bytes(int N, int pass);
+// Sets the dynamic shared-memory limits of the FFT kernels for size N (call before capture).
+template <class T> void fft_prepare(int N);
+
+// Fused FP32 form (fused.cu).
+void launch_fused_rhs(const Group<float>& g, int par, cudaStream_t st);
+void launch_fused_correct(const Group<float>& g, int par, cudaStream_t st);
+bool fused_supported(int N);
+
+}  // namespace ttsh

@@ -1,0 +1,159 @@
+/* ttsh.h — C ABI of libttsh, the GB300 (sm_103a) implementation of the TTSH3D timestep.
+ *
+ * The reference program (Sherlocked-L/Bacterial-Droplet, bacterial_droplet_12-16/TTSH3D.cu)
+ * has no library interface: its path is the executable TTSH3D.out driven by run_cuda.pl,
+ * reading data_<gpu_node>/input.dat and writing data_<gpu_node>/conf_<te>.dat. Each entry
+ * point below replaces one host routine of that program (cited as file:line) so that a
+ * thin main() — bacterial-droplet_gb300/shim/TTSH3D.cu — reproduces the program's
+ * behaviour, and other callers (ctypes, cgo, JNI) can drive many droplets per launch.
+ *
+ * Conventions
+ *   - Every call returns an int status: TTSH_OK (0) or a TTSH_E_* code; no exceptions cross
+ *     the ABI. ttsh_strerror() maps a code to text; ttsh_last_error() gives the last message.
+ *   - Host arrays are unpadded N^3 float64, x fastest: index (z*N + y)*N + x. The reference's
+ *     device arrays carry an Nb-wide periodic halo (TTSH3D.cu:1127-1272); here the halo is
+ *     implicit (periodic index wrap inside the kernels).
+ *   - The library owns all device memory. A handle is used by one host thread at a time.
+ *   - ttsh_step() is asynchronous on the handle's stream; get/reduce/write calls synchronise.
+ */
+#ifndef TTSH_H
+#define TTSH_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TTSH_OK 0
+#define TTSH_E_INVALID 1      /* bad argument or parameter value */
+#define TTSH_E_IO 2           /* file could not be opened / written */
+#define TTSH_E_PARSE 3        /* input.dat malformed or sentinel != -8848 */
+#define TTSH_E_CUDA 4         /* a CUDA runtime call failed */
+#define TTSH_E_NODEVICE 5     /* no CUDA device visible */
+#define TTSH_E_NOMEM 6        /* device or host allocation failed */
+#define TTSH_E_UNSTABLE 7     /* non-finite value detected by the watchdog */
+#define TTSH_E_UNSUPPORTED 8  /* size or option not supported by this build */
+
+#define TTSH_READ_SUCCESS (-8848) /* the reference's sentinel, TTSH3D.cu:748 */
+
+/* The 33 tokens of input.dat, in file order (written by run_cuda.pl:53-86, read by
+ * GetInput, TTSH3D.cu:696-752). Names and order are the reference's. */
+typedef struct ttsh_input {
+  int TimeScheme, RKStage, ExplImpi, AdapTime, ExpoData, InitCond, isSimplified, checkUnStable;
+  int Nx, Ny, Nz, Nb;
+  double h, dt0, T0, Ts, dte, dtVarC, dtMax;
+  double mu, cA, alpha, beta, eta, La, kappa, lambda0, aPhi, kPhi, gamma, A, init0;
+  int ReadSuccess;
+} ttsh_input;
+
+/* Build-defined options that input.dat does not carry (kept in a separate struct so that
+ * input.dat stays byte-compatible with run_cuda.pl and readDraw.py). */
+#define TTSH_K2_REFERENCE 0   /* continuous k^2, k2[0] = 1 (initPoissonSolver, TTSH3D.cu:1088-1124) */
+#define TTSH_K2_DISCRETE 1    /* modified wavenumber of the 27-point gradient: exactly solenoidal */
+#define TTSH_QUIRK_STALE_HALO 1 /* divergence of u*, P* sees last step's halo (getRHS :369-371) */
+typedef struct ttsh_ext {
+  double zeta;     /* active stress -zeta * div(phi P P); 0 = the reference's physics */
+  double R, xi;    /* droplet radius and interface width of ttsh_init_droplet */
+  uint64_t seed;   /* polarisation seed of ttsh_init_droplet */
+  int precision;   /* 64 = FP64 fields and FFT, 32 = FP32 fields and FFT */
+  int k2_mode;     /* TTSH_K2_REFERENCE or TTSH_K2_DISCRETE */
+  int quirks;      /* bitmask of TTSH_QUIRK_* (default TTSH_QUIRK_STALE_HALO) */
+  int reserved;
+} ttsh_ext;
+
+typedef struct ttsh_stats {
+  double mass;       /* sum(phi) h^3, FP64 reduction */
+  double max_div_u;  /* max |sum_a D_a u_a| after the last projection, FP64 */
+  double max_abs_u;  /* max |u_a| */
+  double T;          /* simulated time */
+  int64_t steps;     /* steps taken since creation */
+  int nonfinite;     /* 1 if any NaN/Inf was seen in phi, P or u */
+  int reserved;
+} ttsh_stats;
+
+typedef struct ttsh_sim ttsh_sim;
+
+/* GetInput (TTSH3D.cu:696-752): parse the 33 whitespace-separated tokens of input.dat.
+ * Returns TTSH_E_PARSE when a token is missing or the sentinel is not -8848 (the reference
+ * prints "Error while reading the input file!" and skips the run, :748-751, :270). */
+int ttsh_read_input(const char* path, ttsh_input* out);
+
+/* Fill `out` with the reference defaults of run_cuda.pl:7-44 (N = 64). */
+void ttsh_default_input(ttsh_input* out);
+void ttsh_default_ext(ttsh_ext* out);
+
+/* MemAlloc + initPoissonSolver + cudaMemcpyToSymbol(p) (TTSH3D.cu:1127-1272, :1088-1124,
+ * :761): one droplet. Requires Nx == Ny == Nz (the reference's FFT plan is valid for cubes
+ * only, :1123). `device` < 0 selects the current device. */
+int ttsh_create(const ttsh_input* in, const ttsh_ext* ext, int device, ttsh_sim** out);
+
+/* Many independent droplets advanced together (one launch per kernel per size group).
+ * `in` and `ext` are arrays of n entries; sizes may differ between instances. */
+int ttsh_batch_create(const ttsh_input* in, const ttsh_ext* ext, int n, int device, ttsh_sim** out);
+
+/* Use a caller stream (cudaStream_t passed as void*); NULL = the library's own stream. */
+int ttsh_set_stream(ttsh_sim* s, void* stream);
+
+/* InitConf (TTSH3D.cu:755-896), host -> device: set instance `inst`'s state from host
+ * arrays. P and u are 3*N^3 (component-major: x, y, z). ustar/Pstar may be NULL (zeros);
+ * they seed the previous-step halo of quirk Q2. */
+int ttsh_set_state(ttsh_sim* s, int inst, const double* phi, const double* P, const double* u,
+                   const double* ustar, const double* Pstar);
+
+/* The build-defined initial condition (host only, no GPU needed): phi = (1 - tanh((r-R)/xi))/2
+ * centred at (N/2,N/2,N/2); P = unit vectors where phi > 0.5 with directions uniform on the
+ * sphere from `seed` (counter-based), 3 Jacobi passes (self + 6 face neighbours, periodic),
+ * then zero where phi <= 0.5; `angular_noise` > 0 adds Gaussian angular noise (radians) to
+ * the initial directions. Replaces InitConf's time(0)-seeded noise (TTSH3D.cu:801-824). */
+int ttsh_init_droplet(int N, double h, double R, double xi, uint64_t seed, double angular_noise,
+                      double* phi, double* P);
+
+/* EEuler x nsteps (TTSH3D.cu:347-359, run/evolve :336-343, :311-331): asynchronous. */
+int ttsh_step(ttsh_sim* s, int nsteps);
+
+/* Block until all queued work on the handle's stream is done; returns a CUDA error if any. */
+int ttsh_sync(ttsh_sim* s);
+
+/* Device -> host copies of ExpoConf (TTSH3D.cu:904-963): any pointer may be NULL.
+ * P, u, ustar, Pstar are 3*N^3; p_v and p_p are the last projection's pressures. */
+int ttsh_get_state(ttsh_sim* s, int inst, double* phi, double* P, double* u, double* p_v, double* p_p);
+int ttsh_get_provisional(ttsh_sim* s, int inst, double* ustar, double* Pstar);
+
+/* FP64 diagnostics (new; the reference has none): mass, divergence, non-finite watchdog. */
+int ttsh_reduce(ttsh_sim* s, int inst, ttsh_stats* out);
+
+/* ExpoConf (TTSH3D.cu:899-1014): write the snapshot text file of instance `inst` at `path`:
+ * one line per site, y outer, x, z inner; columns "vx vy vz px py pz phi" printed as
+ * fixed with 15 decimals (ExpoData == 1) or "vx vy " (ExpoData == -1). */
+int ttsh_write_conf(ttsh_sim* s, int inst, const char* path);
+
+/* Same formatter on host arrays (no GPU): for writing conf files from any source. */
+int ttsh_format_conf(int N, int expo_data, const double* phi, const double* P, const double* u,
+                     const char* path);
+
+/* MemFree + cufftDestroy (TTSH3D.cu:280-281, :1275-1419). */
+void ttsh_destroy(ttsh_sim* s);
+
+const char* ttsh_strerror(int code);
+const char* ttsh_last_error(void);
+
+/* Instances, their sizes, the simulated time. */
+int ttsh_num_instances(const ttsh_sim* s);
+int ttsh_instance_n(const ttsh_sim* s, int inst);
+double ttsh_time(const ttsh_sim* s);
+
+/* Timing helper for benchmarks: runs nsteps steps with a CUDA event pair around every kernel
+ * of the step and returns, per kernel class, the mean device time per step in ms.
+ * names[i] point to static strings. Returns the number of classes written (<= cap). */
+int ttsh_profile_kernels(ttsh_sim* s, int nsteps, int cap, const char** names, double* ms_per_step,
+                         int64_t* launches_per_step);
+
+/* Launch count of one step (kernels of this library). */
+int ttsh_launches_per_step(const ttsh_sim* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TTSH_H */

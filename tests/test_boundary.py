@@ -1,0 +1,166 @@
+"""CPU tests of the drop-in boundary: input.dat (GetInput), the snapshot text layout
+(ExpoConf, readDraw.py), the build-defined initial condition, and the C ABI exports."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT
+
+
+def test_library_exports_every_declared_symbol():
+    import ttsh
+    L = ttsh.lib()
+    syms = ttsh.declared_symbols()
+    assert len(syms) >= 20
+    missing = [s for s in syms if not hasattr(L, s)]
+    assert not missing, missing
+
+
+def test_read_input_golden_from_run_cuda_pl():
+    """input.dat printed by run_cuda.pl:53-87 (tests/golden/input_default.dat) parses to its defaults."""
+    import ttsh
+    got = ttsh.read_input(os.path.join(GOLDEN, "input_default.dat")).as_dict()
+    want = ttsh.default_input().as_dict()
+    assert got == want
+
+
+def test_write_input_is_byte_identical_to_perl(tmp_path):
+    import ttsh
+    p = tmp_path / "input.dat"
+    ttsh.write_input(str(p), ttsh.default_input())
+    assert p.read_bytes() == open(os.path.join(GOLDEN, "input_default.dat"), "rb").read()
+
+
+def test_read_input_sentinel_and_errors(tmp_path):
+    import ttsh
+    toks = open(os.path.join(GOLDEN, "input_default.dat")).read().split()
+    bad = tmp_path / "bad.dat"
+    bad.write_text("\n".join(toks[:-1] + ["-1"]) + "\n")
+    with pytest.raises(ttsh.TTSHError) as e:
+        ttsh.read_input(str(bad))
+    assert e.value.code == ttsh.E_PARSE
+    short = tmp_path / "short.dat"
+    short.write_text("\n".join(toks[:20]) + "\n")
+    with pytest.raises(ttsh.TTSHError) as e:
+        ttsh.read_input(str(short))
+    assert e.value.code == ttsh.E_PARSE
+    with pytest.raises(ttsh.TTSHError) as e:
+        ttsh.read_input(str(tmp_path / "missing.dat"))
+    assert e.value.code == ttsh.E_IO
+    # a float token where the reference reads an int stops the stream, as `>>` does
+    floaty = tmp_path / "floaty.dat"
+    floaty.write_text("\n".join(["1.5"] + toks[1:]) + "\n")
+    with pytest.raises(ttsh.TTSHError):
+        ttsh.read_input(str(floaty))
+
+
+def _fields(N, seed):
+    rng = np.random.default_rng(seed)
+    phi = rng.uniform(-1, 2, (N, N, N))
+    P = rng.standard_normal((3, N, N, N)) * 10.0 ** rng.integers(-20, 3, (3, N, N, N))
+    u = rng.standard_normal((3, N, N, N)) * 1e-3
+    u[0, 0, 0, 0] = -0.0
+    u[1, 0, 0, 0] = 5e-16
+    u[2, 0, 0, 0] = -5e-16
+    return phi, P, u
+
+
+def test_conf_layout_matches_expoconf(tmp_path):
+    """One line per site, y outer, x, z inner; 'vx vy vz px py pz phi' as fixed/setprecision(15)."""
+    import ttsh
+    N = 6
+    phi, P, u = _fields(N, 1)
+    f = tmp_path / "conf_0.dat"
+    ttsh.format_conf(str(f), phi, P, u, expo_data=1)
+    lines = []
+    for y in range(N):
+        for x in range(N):
+            for z in range(N):
+                vals = [u[0, z, y, x], u[1, z, y, x], u[2, z, y, x], P[0, z, y, x], P[1, z, y, x], P[2, z, y, x],
+                        phi[z, y, x]]
+                lines.append(" ".join("%.15f" % v for v in vals) + "\n")
+    assert f.read_text() == "".join(lines)
+    g = tmp_path / "conf_m1.dat"
+    ttsh.format_conf(str(g), phi, P, u, expo_data=-1)
+    want = "".join("%.15f %.15f " % (u[0, z, y, x], u[1, z, y, x])
+                   for y in range(N) for x in range(N) for z in range(N))
+    assert g.read_text() == want
+    e = tmp_path / "conf_e.dat"
+    ttsh.format_conf(str(e), phi, P, u, expo_data=0)
+    assert e.read_text() == ""
+
+
+def test_conf_readdraw_mirror(tmp_path):
+    """numpy restatement of readDraw.py:205-215 (pd.read_csv(sep=' ', names=...), reshape (Ly,Lx,Lz))."""
+    import ttsh
+    N = 8
+    phi, P, u = _fields(N, 2)
+    f = tmp_path / "conf_3.dat"
+    ttsh.format_conf(str(f), phi, P, u)
+    data = np.loadtxt(str(f))
+    names = ["vx", "vy", "vz", "px", "py", "pz", "phi"]
+    cols = {n: data[:, i].reshape((N, N, N)) for i, n in enumerate(names)}
+    # readDraw's array is indexed [y][x][z]; ours is [z][y][x]
+    np.testing.assert_allclose(cols["phi"], np.transpose(phi, (1, 2, 0)), rtol=0, atol=1e-15)
+    np.testing.assert_allclose(cols["vy"], np.transpose(u[1], (1, 2, 0)), rtol=0, atol=1e-15)
+    np.testing.assert_allclose(cols["pz"], np.transpose(P[2], (1, 2, 0)), rtol=0, atol=1e-15 * 1e3)
+
+
+def test_conf_parallel_writer_large(tmp_path):
+    """Multi-chunk path (N large enough for several formatting rounds) stays in loop order."""
+    import ttsh
+    N = 40
+    phi, P, u = _fields(N, 3)
+    f = tmp_path / "big.dat"
+    ttsh.format_conf(str(f), phi, P, u)
+    with open(f) as fh:
+        lines = fh.readlines()
+    assert len(lines) == N ** 3
+    for li in (0, 1, N, N * N, N ** 3 - 1, 12345):
+        y, rem = divmod(li, N * N)
+        x, z = divmod(rem, N)
+        assert float(lines[li].split()[6]) == pytest.approx(phi[z, y, x], abs=1e-15)
+
+
+def test_init_droplet_properties():
+    import ttsh
+    N, R, xi = 32, 8.0, 2.0
+    phi, P = ttsh.init_droplet(N, R, xi, seed=0)
+    z, y, x = np.meshgrid(np.arange(N), np.arange(N), np.arange(N), indexing="ij")
+    r = np.sqrt((x - N / 2) ** 2 + (y - N / 2) ** 2 + (z - N / 2) ** 2)
+    np.testing.assert_allclose(phi, 0.5 * (1 - np.tanh((r - R) / xi)), rtol=0, atol=1e-15)
+    mag = np.sqrt((P ** 2).sum(0))
+    assert np.all(mag[phi <= 0.5] == 0)
+    assert np.all(mag <= 1 + 1e-12)
+    assert (mag[phi > 0.5] > 0).mean() > 0.99
+    phi2, P2 = ttsh.init_droplet(N, R, xi, seed=0)
+    assert np.array_equal(P, P2)
+    _, P3 = ttsh.init_droplet(N, R, xi, seed=1)
+    assert not np.array_equal(P, P3)
+    _, Pn = ttsh.init_droplet(N, R, xi, seed=0, angular_noise=0.01)
+    d = np.abs(Pn - P)[:, phi > 0.5]
+    assert 0 < d.max() < 0.1
+
+
+REF_CONFS = sorted(glob.glob(os.path.join(GOLDEN, "ref_N12_conf_*.dat")))
+
+
+@pytest.mark.skipif(not REF_CONFS, reason="reference golden fixture not generated")
+def test_conf_writer_byte_identical_to_reference_expoconf(tmp_path):
+    """The reference program's own conf_0.dat (written from its initial state) is reproduced byte for byte."""
+    import ttsh
+    g = np.load(os.path.join(GOLDEN, "ref_N12.npz"))
+    conf0 = [c for c in REF_CONFS if c.endswith("conf_0.dat")]
+    assert conf0
+    P = np.stack([g["init_px"], g["init_py"], g["init_pz"]])
+    u = np.stack([g["init_vx"], g["init_vy"], g["init_vz"]])
+    f = tmp_path / "conf_0.dat"
+    ttsh.format_conf(str(f), np.ascontiguousarray(g["init_phi"]), P, u)
+    assert f.read_bytes() == open(conf0[0], "rb").read()
+
+
+def test_golden_fixture_script_is_committed():
+    assert os.path.exists(os.path.join(ROOT, "tests", "golden", "make_ref_golden.py"))
+    assert os.path.exists(os.path.join(ROOT, "tests", "golden", "make_input_dat.py"))
