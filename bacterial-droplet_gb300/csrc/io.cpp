@@ -49,6 +49,15 @@ void ttsh_default_input(ttsh_input* o) {
   o->ReadSuccess = TTSH_READ_SUCCESS;
 }
 
+int ttsh_struct_size(int which) {
+  switch (which) {
+    case 0: return (int)sizeof(ttsh_input);
+    case 1: return (int)sizeof(ttsh_ext);
+    case 2: return (int)sizeof(ttsh_stats);
+    default: return -1;
+  }
+}
+
 void ttsh_default_ext(ttsh_ext* e) {
   if (!e) return;
   std::memset(e, 0, sizeof(*e));

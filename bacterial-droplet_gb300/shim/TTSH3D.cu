@@ -1,0 +1,218 @@
+// TTSH3D.cu — drop-in replacement of the reference program's main() for run_cuda.pl / forEach.pl.
+//
+// run_cuda.pl compiles this file with its own line (run_cuda.pl:4:
+//   nvcc -std=c++14 -I /usr/include/cuda/ -L /usr/lib64/ --cudart=shared -lcufft TTSH3D.cu -o TTSH3D.out)
+// and rewrites line 42 to "int gpu_node = <n>;" (run_cuda.pl:104-105, forEach.pl:114-125),
+// so line 42 below must stay that declaration. The step itself runs in libttsh.so (sm_103a
+// kernels), loaded with dlopen from $TTSH_LIB, or libttsh.so next to the executable, or
+// bacterial-droplet_gb300/lib/libttsh.so relative to it.
+//
+// Behaviour kept from the reference program (TTSH3D.cu of Bacterial-Droplet):
+//   * input: data_<gpu_node>/input.dat, 33 tokens, sentinel -8848 (GetInput :696-752)
+//   * initial state, InitCond == 1: the same uniform noise draws, in the same order and with
+//     the same generator (std::default_random_engine seeded by time(0), or $TTSH_SEED), and
+//     phi = (1 - tanh((r - N/4)*2))/2 (InitConf :798-824); InitCond == 0 reads vx vy from
+//     data/conf_<t0>.dat (:794-797)
+//   * time loop: T += Dt, snapshot conf_<floor(T/dte)>.dat whenever floor(T/dte) increases,
+//     stop when T > Ts, conf_0.dat first when T0 == 0 (evolve :290-332)
+//   * snapshot text layout of ExpoConf (:899-1014)
+// Extensions (environment): TTSH_PRECISION=32|64 (default 64), TTSH_K2=0|1, TTSH_ZETA=<zeta>,
+// TTSH_QUIRKS=<mask> (default 1, the reference's stale-halo divergence).
+#include <dlfcn.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+#include <cmath>
+#include <ctime>
+#include <fstream>
+#include <iostream>
+#include <random>
+#include <string>
+#include <vector>
+
+using namespace std;
+
+// -------------------------------------------------------------------------------------
+// Parameters for this run. The line below is rewritten by run_cuda.pl / forEach.pl.
+//
+// (keep this comment block the same length: the next declaration is line 42)
+int gpu_node = 1;
+
+// Layout-identical copies of the include/ttsh.h structures (checked at run time).
+struct ttsh_input {
+  int TimeScheme, RKStage, ExplImpi, AdapTime, ExpoData, InitCond, isSimplified, checkUnStable;
+  int Nx, Ny, Nz, Nb;
+  double h, dt0, T0, Ts, dte, dtVarC, dtMax;
+  double mu, cA, alpha, beta, eta, La, kappa, lambda0, aPhi, kPhi, gamma, A, init0;
+  int ReadSuccess;
+};
+struct ttsh_ext {
+  double zeta, R, xi;
+  uint64_t seed;
+  int precision, k2_mode, quirks, reserved;
+};
+struct ttsh_sim;
+
+struct Api {
+  int (*read_input)(const char*, ttsh_input*);
+  void (*default_ext)(ttsh_ext*);
+  int (*create)(const ttsh_input*, const ttsh_ext*, int, ttsh_sim**);
+  int (*set_state)(ttsh_sim*, int, const double*, const double*, const double*, const double*, const double*);
+  int (*step)(ttsh_sim*, int);
+  int (*write_conf)(ttsh_sim*, int, const char*);
+  void (*destroy)(ttsh_sim*);
+  const char* (*last_error)(void);
+  int (*struct_size)(int);
+};
+
+static void* load_lib() {
+  std::vector<std::string> cands;
+  if (const char* e = getenv("TTSH_LIB")) cands.push_back(e);
+  char exe[4096];
+  ssize_t n = readlink("/proc/self/exe", exe, sizeof(exe) - 1);
+  if (n > 0) {
+    exe[n] = 0;
+    std::string d(exe);
+    d = d.substr(0, d.find_last_of('/'));
+    cands.push_back(d + "/libttsh.so");
+    cands.push_back(d + "/bacterial-droplet_gb300/lib/libttsh.so");
+    cands.push_back(d + "/../bacterial-droplet_gb300/lib/libttsh.so");
+  }
+  cands.push_back("libttsh.so");
+  for (auto& c : cands) {
+    void* h = dlopen(c.c_str(), RTLD_NOW | RTLD_LOCAL);
+    if (h) return h;
+  }
+  cout << "TTSH3D: cannot load libttsh.so (set TTSH_LIB): " << dlerror() << endl;
+  return nullptr;
+}
+
+template <class F>
+static bool sym(void* h, const char* name, F& f) {
+  f = reinterpret_cast<F>(dlsym(h, name));
+  if (!f) cout << "TTSH3D: libttsh.so lacks " << name << endl;
+  return f != nullptr;
+}
+
+static double env_d(const char* k, double d) { const char* v = getenv(k); return v ? atof(v) : d; }
+static int env_i(const char* k, int d) { const char* v = getenv(k); return v ? atoi(v) : d; }
+
+static void progress(double T, double T0, double Ts, clock_t t0) {
+  double pr = (T - T0) / (Ts - T0);
+  int w = 50, pos = (int)(w * pr);
+  cout << "Progress: [";
+  for (int i = 0; i < w; ++i) cout << (i < pos ? "=" : (i == pos ? ">" : " "));
+  double used = double(clock() - t0) / CLOCKS_PER_SEC;
+  cout << "] " << int(pr * 100.0) << " %";
+  if (T == 0) cout << "\r";
+  else cout << ".  " << floor(used / pr * (1 - pr)) << "s remains.\r";
+  cout.flush();
+}
+
+int main() {
+  clock_t tStart = clock();
+  void* h = load_lib();
+  if (!h) return 1;
+  Api a;
+  if (!(sym(h, "ttsh_read_input", a.read_input) && sym(h, "ttsh_default_ext", a.default_ext) &&
+        sym(h, "ttsh_create", a.create) && sym(h, "ttsh_set_state", a.set_state) && sym(h, "ttsh_step", a.step) &&
+        sym(h, "ttsh_write_conf", a.write_conf) && sym(h, "ttsh_destroy", a.destroy) &&
+        sym(h, "ttsh_last_error", a.last_error) && sym(h, "ttsh_struct_size", a.struct_size)))
+    return 1;
+  if (a.struct_size(0) != (int)sizeof(ttsh_input) || a.struct_size(1) != (int)sizeof(ttsh_ext)) {
+    cout << "TTSH3D: libttsh.so structure layout mismatch" << endl;
+    return 1;
+  }
+  const std::string dir = "data_" + to_string(gpu_node);
+  ttsh_input P;
+  int rc = a.read_input((dir + "/input.dat").c_str(), &P);
+  cout << "hhhhhhhhhhh:" << P.ReadSuccess << endl;  // the reference prints the sentinel it read
+  if (rc != 0) {
+    cout << "Error while reading the input file!" << endl;
+    clock_t tEnd = clock();
+    cout << "Simulation finished. CPU time = " << double(tEnd - tStart) / CLOCKS_PER_SEC << " sec" << endl;
+    return 0;
+  }
+  ttsh_ext ext;
+  a.default_ext(&ext);
+  ext.precision = env_i("TTSH_PRECISION", 64);
+  ext.k2_mode = env_i("TTSH_K2", 0);
+  ext.zeta = env_d("TTSH_ZETA", 0.0);
+  ext.quirks = env_i("TTSH_QUIRKS", 1);
+  ttsh_sim* sim = nullptr;
+  rc = a.create(&P, &ext, -1, &sim);
+  if (rc != 0) {
+    cout << "TTSH3D: " << a.last_error() << endl;
+    return 2;
+  }
+  const int N = P.Nx;
+  const size_t n = (size_t)N * N * N;
+  std::vector<double> phi(n, 0.0), Pf(3 * n, 0.0), u(3 * n, 0.0), us(3 * n, 0.0), Ps(3 * n, 0.0);
+  // InitConf (TTSH3D.cu:755-896): x outer, y, z inner; 14 draws per site in the reference order.
+  default_random_engine rng(getenv("TTSH_SEED") ? (unsigned)atol(getenv("TTSH_SEED")) : (unsigned)time(0));
+  uniform_real_distribution<double> randUR;
+  int t0 = (P.T0 + 0.1 * P.dte) / P.dte;
+  ifstream InputFile("data/conf_" + to_string(t0) + ".dat");
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < N; j++)
+      for (int k = 0; k < N; k++) {
+        const size_t idx = ((size_t)k * N + j) * N + i;
+        if (P.InitCond == 0) {
+          InputFile >> u[idx] >> u[n + idx];
+        } else if (P.InitCond == 1) {
+          double* tgt[12] = {&u[idx], &u[n + idx], &u[2 * n + idx], &us[idx], &us[n + idx], &us[2 * n + idx],
+                             &Pf[idx], &Pf[n + idx], &Pf[2 * n + idx], &Ps[idx], &Ps[n + idx], &Ps[2 * n + idx]};
+          for (int c = 0; c < 12; ++c) *tgt[c] = 0 + P.init0 * (randUR(rng) - 0.5);
+          double dx = (i - P.Nx / 2.), dy = (j - P.Ny / 2.), dz = (k - P.Nz / 2.);
+          double r = sqrt(dx * dx + dy * dy + dz * dz);
+          phi[idx] = (1 - tanh((r - P.Nx / 4.) * 2)) / 2;
+          (void)randUR(rng);  // p_v: overwritten by the first projection
+          (void)randUR(rng);  // p_p
+        }
+      }
+  rc = a.set_state(sim, 0, phi.data(), Pf.data(), u.data(), us.data(), Ps.data());
+  if (rc != 0) {
+    cout << "TTSH3D: " << a.last_error() << endl;
+    return 2;
+  }
+  // evolve (TTSH3D.cu:290-332); steps between snapshots are issued as one call.
+  double T = P.T0, Dt = P.dt0;
+  progress(T, P.T0, P.Ts, tStart);
+  if (P.T0 == 0) {
+    if ((rc = a.write_conf(sim, 0, (dir + "/conf_0.dat").c_str())) != 0) {
+      cout << "TTSH3D: " << a.last_error() << endl;
+      return 2;
+    }
+  }
+  bool stop = false;
+  while (!stop) {
+    int pending = 0;
+    long te = -1;
+    for (;;) {
+      T = T + Dt;
+      ++pending;
+      if (floor(T / P.dte) > floor((T - Dt) / P.dte)) { te = (long)floor(T / P.dte); }
+      if (T > P.Ts) stop = true;
+      if (te >= 0 || stop || pending >= 1000000) break;
+    }
+    if ((rc = a.step(sim, pending)) != 0) {
+      cout << "TTSH3D: " << a.last_error() << endl;
+      return 2;
+    }
+    if (te >= 0) {
+      if ((rc = a.write_conf(sim, 0, (dir + "/conf_" + to_string(te) + ".dat").c_str())) != 0) {
+        cout << "TTSH3D: " << a.last_error() << endl;
+        return 2;
+      }
+      progress(T, P.T0, P.Ts, tStart);
+    }
+  }
+  a.destroy(sim);
+  clock_t tEnd = clock();
+  cout << "Simulation finished. ";
+  cout << "CPU time = " << double(tEnd - tStart) / CLOCKS_PER_SEC << " sec" << endl;
+  return 0;
+}

@@ -101,6 +101,7 @@ def lib():
             "ttsh_profile_kernels": ([_VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), _D,
                                       ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
             "ttsh_launches_per_step": ([_VP], ctypes.c_int),
+            "ttsh_struct_size": ([ctypes.c_int], ctypes.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

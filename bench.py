@@ -1,0 +1,378 @@
+"""Benchmark of the TTSH3D timestep on GB300: lattice-site-steps per second.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--precision 32|64] [--workload NAME]
+
+Workload (default "2x256"): the 256^3 droplet case, run as two droplets in one
+batch (zeta = 0.005 and 0.02, R = 64, xi = 2, seed 1, reference constants,
+reference physics: continuous k^2 and the stale-halo divergence), FP32 fields and
+FFT. "1x256" is one droplet (zeta 0.02); "64x128" is the 64-droplet sweep of 128^3
+boxes; "24mixed" is 24 droplets of 96/128/160/192^3; "1x512" the single 512^3 droplet.
+
+The metric is Msite*steps/s = (sum over droplets of N^3) * steps / seconds / 1e6,
+timed with CUDA events on the library's stream around exactly K steps after W
+warm-up steps. The fields (>= 1.2 GB per 256^3 droplet in FP32) are far larger
+than L2 (~126 MB), so no L2 flush is needed between steps.
+
+--impl reference times the reference program itself (TTSH3D.cu, patched only in
+init/dump/timing, built with its own nvcc line; one 256^3 droplet, FP64, zeta=0,
+on the same GPU). If that program is not built, the FP64 C++/OpenMP restatement
+of the same step is timed on the host cores instead.
+
+Under torchrun (N > 1) every rank runs its own replica of the workload (the path
+has no exchange between droplets): weak scaling, time = max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "bacterial-droplet_gb300"), os.path.join(ROOT, "oracle"),
+           os.path.join(ROOT, "tests", "golden")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Msite·steps/s at 256³, batched FP32 vs plain FP64 on one GB300; %HBM peak"
+UNIT = "Msite*steps/s"
+# Algorithmic words (one scalar per site) per site-step of each kernel class; 34 in total for
+# the three-phase schedule (fused_rhs 16, the FFT round trip 8 for two scalars, fused_correct 14),
+# B_alg = 136 B in FP32, 272 B in FP64.
+B_ALG_WORDS = 34
+KERNEL_WORDS = {
+    "fused_rhs": 16,        # reads phi, P, u (7); writes phi', u*, P* (7) and the packed source (2)
+    "fused_correct": 14,    # reads u*, P* (6) and the packed pressure (2); writes u, P (6)
+    "stage1": 17, "stage2": 27, "div": 8, "correct": 14,
+    "fft_x_fwd": 4, "fft_y_fwd": 4, "fft_z_poisson": 4, "fft_y_inv": 4, "fft_x_inv": 4,
+}
+
+
+def workload(name: str):
+    """List of droplets: (N, R, xi, seed, zeta)."""
+    if name == "2x256":
+        return [(256, 64.0, 2.0, 1, 0.005), (256, 64.0, 2.0, 1, 0.02)]
+    if name == "1x256":
+        return [(256, 64.0, 2.0, 1, 0.02)]
+    if name == "64x128":
+        rng = np.random.default_rng(2024)
+        R = rng.uniform(20, 40, 64)
+        z = np.exp(rng.uniform(np.log(1e-3), np.log(5e-2), 64))
+        return [(128, float(R[i]), 2.0, 100 + i, float(z[i])) for i in range(64)]
+    if name == "24mixed":
+        out = []
+        for k, L in enumerate((96, 128, 160, 192)):
+            for j in range(6):
+                i = 6 * k + j
+                out.append((L, 0.3 * L, 2.0, 200 + i, 0.01 if i % 2 == 0 else 0.03))
+        return out
+    if name == "1x512":
+        return [(512, 160.0, 3.0, 7, 0.02)]
+    if name == "1x64":
+        return [(64, 16.0, 2.0, 0, 0.01)]
+    raise SystemExit("unknown workload " + name)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        os.unlink(self.path)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            if len(r) >= 9:
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower() == "active":
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            return float(json.load(open(p))["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def make_sim(ttsh, drops, precision, k2_mode=0, quirks=1):
+    inps, exts = [], []
+    for (N, R, xi, seed, zeta) in drops:
+        inps.append(ttsh.default_input(Nx=N, Ny=N, Nz=N))
+        exts.append(ttsh.default_ext(precision=precision, zeta=zeta, R=R, xi=xi, seed=seed, k2_mode=k2_mode,
+                                     quirks=quirks))
+    return ttsh.Sim(inps, exts, device=0)
+
+
+def init_states(ttsh, drops, pinned: bool):
+    import torch
+    states = []
+    cache = {}
+    for (N, R, xi, seed, zeta) in drops:
+        key = (N, R, xi, seed)
+        if key not in cache:
+            phi, P = ttsh.init_droplet(N, R, xi, seed)
+            if pinned:
+                tp = torch.empty((N, N, N), dtype=torch.float64, pin_memory=True)
+                tq = torch.empty((3, N, N, N), dtype=torch.float64, pin_memory=True)
+                tu = torch.zeros((3, N, N, N), dtype=torch.float64, pin_memory=True)
+                tp.numpy()[:] = phi
+                tq.numpy()[:] = P
+                cache[key] = (tp.numpy(), tq.numpy(), tu.numpy(), (tp, tq, tu))
+            else:
+                cache[key] = (phi, P, np.zeros((3, N, N, N)), None)
+        states.append(cache[key])
+    return states
+
+
+def cpu_baseline_sample():
+    """The FP64 oracle (C++/OpenMP restatement) on one 256^3 droplet for 2 steps, host cores."""
+    import oracle
+    import ttsh
+    oracle.build()
+    n = oracle.set_threads(os.cpu_count() or 1)
+    N, steps = 256, 2
+    phi, P = ttsh.init_droplet(N, 64.0, 2.0, 1)
+    s = oracle.new_state(N)
+    s["phi"][:] = phi
+    s["px"][:], s["py"][:], s["pz"][:] = P
+    t0 = time.perf_counter()
+    oracle.step(s, steps, N, zeta=0.005)
+    dt = time.perf_counter() - t0
+    return {"value": N ** 3 * steps / dt / 1e6, "unit": UNIT, "cores": n, "kind": "port",
+            "sample": "FP64 C++/OpenMP restatement of the step, one 256^3 droplet (zeta=0.005), %d steps, %.1f s"
+                      % (steps, dt)}
+
+
+def run_reference(args):
+    """--impl reference: the reference program on the GPU, else the oracle port on the host."""
+    out = {"metric": METRIC, "unit": UNIT, "impl": "reference", "higher_is_better": True, "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "scaling": "weak", "vs_baseline": None, "data": "synthetic"}
+    binary = None
+    try:
+        import make_ref
+        binary = make_ref.build()
+    except Exception as e:  # report and fall back
+        out["note"] = "reference program not built: %s" % str(e)[:200]
+    if binary:
+        import make_ref_golden as G
+        import ttsh
+        N = 256
+        phi, P = ttsh.init_droplet(N, 64.0, 2.0, 1)
+        st = {k: np.zeros((N, N, N)) for k in G.FIELDS}
+        st["phi"] = phi
+        st["px"], st["py"], st["pz"] = P
+        with tempfile.TemporaryDirectory() as d:
+            t0 = time.perf_counter()
+            log = G.run_reference(binary, d, N, st, Ts=(args.warmup + args.steps - 0.5) * 0.002, dte=1e9, expo=0,
+                                  warmup=args.warmup, nfields=7)
+            wall = time.perf_counter() - t0
+        line = [l for l in log.splitlines() if l.startswith("TTSH_REF_TIMING")][-1]
+        kv = dict(x.split("=") for x in line.split()[1:])
+        steps, sec = int(kv["steps"]), float(kv["seconds"])
+        v = N ** 3 * steps / sec / 1e6
+        out.update(value=v, ms_per_step=1e3 * sec / steps, dtype="f64",
+                   config={"workload": "1 droplet x 256^3 (R=64, xi=2, seed 1, zeta=0: the reference has no "
+                                       "active stress), reference program TTSH3D.cu on the GPU",
+                           "build": "nvcc -std=c++14 --cudart=shared -lcufft (run_cuda.pl:4), no -arch",
+                           "timing": "cudaDeviceSynchronize + steady_clock around the step loop after warm-up",
+                           "process_wall_s": round(wall, 1)},
+                   cpu_baseline={"value": v, "unit": UNIT, "cores": 0, "kind": "reference",
+                                 "sample": "the reference program's own step loop on the GPU (it has no CPU "
+                                           "path), %d steps at 256^3" % steps},
+                   e2e={"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
+    else:
+        cb = cpu_baseline_sample()
+        out.update(value=cb["value"], dtype="f64", config={"workload": "oracle port, " + cb["sample"]},
+                   cpu_baseline=cb, e2e={"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                                         "d2h_bytes_per_step": 0})
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", type=int, default=32, choices=[32, 64])
+    ap.add_argument("--workload", default="2x256")
+    ap.add_argument("--k2", type=int, default=0, choices=[0, 1])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        raise SystemExit("--warmup must be >= 3")
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import ttsh
+
+    drops = workload(args.workload)
+    sites = sum(d[0] ** 3 for d in drops)
+    sim = make_sim(ttsh, drops, args.precision, k2_mode=args.k2)
+    # one non-default stream shared by the library and the timing events
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sim.set_stream(stream.cuda_stream)
+    states = init_states(ttsh, drops, pinned=False)
+    for i, (phi, P, u, _) in enumerate(states):
+        sim.set_state(i, phi, P, u)
+    sim.step(args.warmup)
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    sim.step(args.steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = sites * world * args.steps / (ms / 1e3) / 1e6
+    stats = [sim.reduce(i, check=False) for i in range(len(drops))]
+
+    # per-kernel device times (events around each launch on the library's stream)
+    prof = sim.profile_kernels(20)
+    torch.cuda.synchronize()
+    wbytes = 4 if args.precision == 32 else 8
+    peak, peak_kind = measured_peak_hbm()
+    dom = max(prof.items(), key=lambda kv: kv[1][0])
+    dom_name, (dom_ms, dom_launches) = dom
+    dom_bytes = KERNEL_WORDS.get(dom_name, 0) * wbytes * sites
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
+    launches = sim.launches_per_step()
+
+    # end to end through the public API: host state -> device, K steps each followed by the
+    # FP64 mass/divergence read-back, final state -> host
+    e2e = None
+    if not args.no_e2e:
+        pin = init_states(ttsh, drops, pinned=True)
+        outs = [(np.empty((N, N, N)), np.empty((3, N, N, N)), np.empty((3, N, N, N))) for (N, *_r) in drops]
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for i, (phi, P, u, _) in enumerate(pin):
+            sim.set_state(i, phi, P, u)
+        for _ in range(args.steps):
+            sim.step(1)
+            for i in range(len(drops)):
+                sim.reduce(i, check=False)
+        for i, (phi, P, u) in enumerate(outs):
+            lib_rc = ttsh.lib().ttsh_get_state(sim.handle, i, ttsh._p(phi), ttsh._p(P), ttsh._p(u), None, None)
+            ttsh._check(lib_rc)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([wall], device="cuda", dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            wall = float(t.item())
+        h2d = sum(7 * d[0] ** 3 * 8 for d in drops)
+        d2h = args.steps * len(drops) * 4 * 8 * 256 + sum(7 * d[0] ** 3 * 8 for d in drops)
+        e2e = {"value": sites * world * args.steps / wall / 1e6, "unit": UNIT,
+               "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+               "note": "public API (ttsh.Sim): set_state from pinned host FP64 arrays, %d x (step + FP64 "
+                       "mass/divergence read-back per droplet), get_state of all fields; wall clock" % args.steps}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_sample()
+
+    if rank == 0:
+        hbm_frac = value * 1e6 * B_ALG_WORDS * wbytes / (peak * 1e9)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if args.precision == 32 else "f64", "data": "synthetic",
+            "config": {"workload": args.workload + ": " + ", ".join(
+                "%d^3 (R=%g, xi=%g, seed %d, zeta=%g)" % d for d in drops[:4]) + (" ..." if len(drops) > 4 else ""),
+                "droplets": len(drops), "sites_per_gpu": sites, "form": "fused" if "fused_rhs" in prof else "plain",
+                "physics": "reference (continuous k^2, stale-halo divergence)" if args.k2 == 0 else "discrete k^2",
+                "l2": "inputs larger than L2 (%.1f GB of fields per GPU)" % (sites * 22 * wbytes / 1e9),
+                "parallelism": "replicas" if world > 1 else "1 GPU"},
+            "hbm_pct_of_step": 100 * hbm_frac,
+            "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
+                         peak_kind, "bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms / max(1, dom_launches)},
+            "kernels_ms_per_step": {k: round(v[0], 4) for k, v in prof.items()},
+            "gpu_launches": launches * args.steps,
+            "launches_per_step": launches,
+            "clocks": clocks,
+            "mass": [s["mass"] for s in stats],
+            "max_div_u": [s["max_div_u"] for s in stats],
+        }
+        if e2e:
+            line["e2e"] = e2e
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line))
+    sim.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -150,6 +150,10 @@ double ttsh_time(const ttsh_sim* s);
 int ttsh_profile_kernels(ttsh_sim* s, int nsteps, int cap, const char** names, double* ms_per_step,
                          int64_t* launches_per_step);
 
+/* sizeof(ttsh_input) for which == 0, sizeof(ttsh_ext) for 1, sizeof(ttsh_stats) for 2, else -1:
+ * lets a caller that re-declares the structures (the TTSH3D.cu shim) check the layout. */
+int ttsh_struct_size(int which);
+
 /* Launch count of one step (kernels of this library). */
 int ttsh_launches_per_step(const ttsh_sim* s);
 
