@@ -12,6 +12,7 @@ previously generated file. The step itself (getRHS, getVStar, getP, getStream,
 getVNew, the stencils, BounPeriU, initPoissonSolver) is left byte-identical.
 
 Patches (each anchor must occur exactly once):
+  0. the RNG seed (TTSH3D.cu:40) is $TTSH_SEED when set, else time(0) as in the reference.
   1. InitConf (TTSH3D.cu:755-896): after the reference's own random init, the
      fields are overwritten from data_<gpu_node>/init.bin when that file exists
      (int32 N, int32 nfields, then nfields unpadded N^3 float64 arrays in the
@@ -108,6 +109,9 @@ static void ttshref_dump_final() {
 '''
 
 PATCHES = [
+    # 0. seed: $TTSH_SEED when set, else the reference's time(0) (TTSH3D.cu:40)
+    ("int seed = time(0);\n", "int seed = getenv(\"TTSH_SEED\") ? atoi(getenv(\"TTSH_SEED\")) : time(0);\n"),
+    ('#include "cuda_runtime.h"\n', '#include <cstdlib>\n#include "cuda_runtime.h"\n'),
     # 1. helpers after the global declarations (before main)
     ("//=======================================================================\nint main()\n",
      HELPERS + "//=======================================================================\nint main()\n"),
