@@ -102,6 +102,8 @@ def lib():
                                       ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
             "ttsh_launches_per_step": ([_VP], ctypes.c_int),
             "ttsh_struct_size": ([ctypes.c_int], ctypes.c_int),
+            "ttsh_step_noalloc": ([ctypes.POINTER(Input), ctypes.POINTER(Ext), ctypes.c_int] + [_VP] * 7 + [_VP],
+                                  ctypes.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)

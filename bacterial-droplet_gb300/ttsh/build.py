@@ -17,7 +17,7 @@ LIBDIR = os.path.join(PKG, "lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libttsh.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cu", "plain.cu", "fft.cu", "fused.cu", "io.cpp"]
+SOURCES = ["api.cu", "plain.cu", "fft.cu", "fused.cu", "io.cpp", "noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -157,6 +157,29 @@ int ttsh_struct_size(int which);
 /* Launch count of one step (kernels of this library). */
 int ttsh_launches_per_step(const ttsh_sim* s);
 
+/* Largest grid ttsh_step_noalloc accepts (its fixed working memory is sized for it). */
+#define TTSH_NOALLOC_MAX_N 32
+
+/* ttsh_step_noalloc — no counterpart in the reference (which allocates all its arrays in
+ * MemAlloc). For callers that cannot allocate device memory: their device memory belongs to
+ * another allocator or is capped per process, or they cannot afford cudaFree's device-wide
+ * wait. Advances one droplet `nsteps` explicit steps in FP64 (the plain form, the same kernels
+ * and results as ttsh_step) and allocates nothing: the caller passes DEVICE pointers to its
+ * own FP64 arrays, and the step's working memory is one fixed array inside libttsh
+ * (about 5.8 MB, present on every GPU that loads the library until the process exits).
+ *   phi (N^3), P, u (3*N^3): state, updated in place.
+ *   ustar, Pstar (3*N^3): on entry the previous step's u*, P* (zeros at the start; they feed the
+ *     stale-halo divergence), on return this call's last u*, P*.
+ *   p_v, p_p (N^3): outputs, the last projection's pressures (untouched when nsteps == 0).
+ *   stream: cudaStream_t as void* (NULL = legacy default stream); the call is asynchronous.
+ * Rejects N > TTSH_NOALLOC_MAX_N, non-cubic grids and precision != 64 with TTSH_E_UNSUPPORTED.
+ * All calls share the working array and leave its contents behind (nothing in it must start
+ * at zero); calls whose GPU work overlaps race on it and must be serialised by the caller.
+ * The first call on a device looks up the array's device address and sets kernel attributes;
+ * make that first call before starting any stream capture on the calling thread. */
+int ttsh_step_noalloc(const ttsh_input* in, const ttsh_ext* ext, int nsteps, double* phi, double* P, double* u,
+                      double* ustar, double* Pstar, double* p_v, double* p_p, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
