@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <stdexcept>
@@ -60,9 +61,9 @@ std::vector<int> radix_plan(int N) {
 
 // Kernel classes reported by ttsh_profile_kernels.
 enum KClass { K_STAGE1, K_STAGE2, K_DIV, K_FFT0, K_FFT1, K_FFT2, K_FFT3, K_FFT4, K_CORRECT, K_FUSED_RHS,
-              K_FUSED_CORRECT, K_NCLASS };
+              K_FUSED_DIV, K_FUSED_CORRECT, K_NCLASS };
 const char* kNames[K_NCLASS] = {"stage1", "stage2", "div", "fft_x_fwd", "fft_y_fwd", "fft_z_poisson", "fft_y_inv",
-                                "fft_x_inv", "correct", "fused_rhs", "fused_correct"};
+                                "fft_x_inv", "correct", "fused_rhs", "fused_div", "fused_correct"};
 
 struct Prof {
   cudaStream_t st;
@@ -107,6 +108,7 @@ struct Engine {
       };
       if (fused) {
         run(K_FUSED_RHS, [&] { launch_fused_rhs_t(g, par, st); });
+        run(K_FUSED_DIV, [&] { launch_fused_div_t(g, par, st); });
       } else {
         run(K_STAGE1, [&] { launch_stage1<T>(g, par, st); });
         run(K_STAGE2, [&] { launch_stage2<T>(g, par, st); });
@@ -118,15 +120,22 @@ struct Engine {
     }
   }
   void launch_fused_rhs_t(const Group<T>& g, int par, cudaStream_t st);
+  void launch_fused_div_t(const Group<T>& g, int par, cudaStream_t st);
   void launch_fused_correct_t(const Group<T>& g, int par, cudaStream_t st);
-  int launches(bool fused) const { return (int)groups.size() * (fused ? 7 : 9); }
+  int launches(bool fused) const { return (int)groups.size() * (fused ? 8 : 9); }
 };
 
 template <>
 void Engine<float>::launch_fused_rhs_t(const Group<float>& g, int par, cudaStream_t st) { launch_fused_rhs(g, par, st); }
 template <>
+void Engine<float>::launch_fused_div_t(const Group<float>& g, int par, cudaStream_t st) { launch_fused_div(g, par, st); }
+template <>
 void Engine<float>::launch_fused_correct_t(const Group<float>& g, int par, cudaStream_t st) {
   launch_fused_correct(g, par, st);
+}
+template <>
+void Engine<double>::launch_fused_div_t(const Group<double>&, int, cudaStream_t) {
+  throw std::runtime_error("fused form is FP32 only");
 }
 template <>
 void Engine<double>::launch_fused_rhs_t(const Group<double>&, int, cudaStream_t) {
@@ -155,6 +164,8 @@ struct ttsh_sim {
   int64_t steps = 0;
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   std::vector<void*> tables;  // shared per-N tables
+  double* post = nullptr;     // snapshot-reduction scratch (allocated on first use)
+  size_t post_bytes = 0;
 
   template <class F>
   void with_engine(F&& f) {
@@ -304,6 +315,8 @@ void build_engine(ttsh_sim* s, Engine<T>& E) {
   }
   for (size_t g = 0; g < E.members.size(); ++g) {
     Group<T> G{};
+    const char* fk = std::getenv("TTSH_FFT");  // "stockham": shared-memory Stockham passes only
+    G.fft_kind = (fk && std::string(fk) == "stockham") ? 1 : 0;
     G.n = (int)E.members[g].size();
     G.N = s->inst[E.members[g][0]].N;
     std::vector<InstDev<T>> arr;
@@ -345,6 +358,7 @@ void release(ttsh_sim* s) {
   for (auto& ih : s->inst)
     if (ih.arena) cudaFree(ih.arena);
   for (void* p : s->tables) cudaFree(p);
+  if (s->post) cudaFree(s->post);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
   delete s;
 }
@@ -367,6 +381,14 @@ bool fused_ok(const ttsh_sim* s) {
   for (auto& ih : s->inst)
     if (!fused_supported(ih.N)) return false;
   return true;
+}
+
+// TTSH_FORM_* of the batch: 0 = plain, 1 = fused, -1 = fused requested but unsupported.
+int pick_form(const ttsh_sim* s) {
+  const int want = s->inst[0].ext.form;
+  if (want == TTSH_FORM_PLAIN) return 0;
+  if (want == TTSH_FORM_FUSED) return fused_ok(s) ? 1 : -1;
+  return fused_ok(s) ? 1 : 0;
 }
 
 }  // namespace
@@ -397,6 +419,18 @@ static void d2h(double* dst, const T* src, size_t n, cudaStream_t st, size_t str
   }
 }
 
+// The 13 state arrays of a checkpoint, in file order, as device pointers of the current parity.
+template <class E>
+static std::vector<void*> state_arrays(ttsh_sim* s, E& eng, int inst) {
+  auto& I = eng.h[inst];
+  std::vector<void*> a = {I.phi[s->par]};
+  for (int b = 0; b < 3; ++b) a.push_back(I.P[b]);
+  for (int b = 0; b < 3; ++b) a.push_back(I.U[b]);
+  for (int b = 0; b < 3; ++b) a.push_back(I.Us[s->par][b]);
+  for (int b = 0; b < 3; ++b) a.push_back(I.Ps[s->par][b]);
+  return a;
+}
+
 extern "C" {
 
 int ttsh_batch_create(const ttsh_input* in, const ttsh_ext* ext, int n, int device, ttsh_sim** out) {
@@ -409,6 +443,8 @@ int ttsh_batch_create(const ttsh_input* in, const ttsh_ext* ext, int n, int devi
     if (rc) return rc;
     if ((ext ? ext[i].precision : dflt.precision) != (ext ? ext[0].precision : dflt.precision))
       return set_error(TTSH_E_INVALID, "all instances of a batch share one precision");
+    if ((ext ? ext[i].form : dflt.form) != (ext ? ext[0].form : dflt.form))
+      return set_error(TTSH_E_INVALID, "all instances of a batch share one form");
   }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -432,7 +468,14 @@ int ttsh_batch_create(const ttsh_input* in, const ttsh_ext* ext, int n, int devi
         s->inst[i].N = in[i].Nx;
         s->inst[i].T = in[i].T0;
       }
-      s->fused = fused_ok(s);
+      const int form = pick_form(s);
+      if (form < 0) {
+        release(s);
+        s = nullptr;
+        return set_error(TTSH_E_UNSUPPORTED, "fused form needs FP32 and N a multiple of 32");
+      }
+      s->fused = form == 1;
+      if (s->fused) fused_prepare();
       if (s->precision == 32) build_engine<float>(s, s->ef);
       else build_engine<double>(s, s->ed);
       capture_graphs(s);
@@ -624,6 +667,199 @@ int ttsh_write_conf(ttsh_sim* s, int inst, const char* path) {
   rc = ttsh_get_state(s, inst, phi.data(), P.data(), u.data(), nullptr, nullptr);
   if (rc) return rc;
   return ttsh_format_conf(N, s->inst[inst].in.ExpoData, phi.data(), P.data(), u.data(), path);
+}
+
+int ttsh_snapshot_slice(ttsh_sim* s, int inst, double* centroid, int* index, double* slices) {
+  int rc = check_inst(s, inst);
+  if (rc) return rc;
+  return guarded([&]() -> int {
+    CK(cudaSetDevice(s->device));
+    const int N = s->inst[inst].N;
+    const size_t NN = (size_t)N * N;
+    const size_t need = (9 * NN + 4 * (size_t)centroid_blocks()) * sizeof(double);
+    if (s->post_bytes < need) {
+      CK(cudaStreamSynchronize(s->stream));
+      if (s->post) CK(cudaFree(s->post));
+      s->post = nullptr;
+      CK(cudaMalloc(&s->post, need));
+      s->post_bytes = need;
+    }
+    double* part = s->post + 9 * NN;
+    std::vector<double> hp(4 * (size_t)centroid_blocks());
+    double c[3];
+    int idx[3];
+    s->with_engine([&](auto& E) {
+      const auto& g = E.groups[E.grp[inst]];
+      launch_centroid(g.d_inst, E.loc[inst], s->par, part, s->stream);
+      CK(cudaMemcpyAsync(hp.data(), part, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+      CK(cudaStreamSynchronize(s->stream));
+      double a[4] = {0, 0, 0, 0};
+      for (size_t b = 0; b < hp.size() / 4; ++b)
+        for (int q = 0; q < 4; ++q) a[q] += hp[4 * b + q];
+      for (int q = 0; q < 3; ++q) {
+        c[q] = a[q + 1] / a[0];
+        idx[q] = (int)c[q];  // Python int(): truncation toward zero
+      }
+      if (slices) {
+        const int zs = ((idx[2] % N) + N) % N;
+        launch_slice(g.d_inst, E.loc[inst], s->par, N, zs, s->post, s->stream);
+        CK(cudaMemcpyAsync(slices, s->post, 9 * NN * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+      }
+    });
+    for (int q = 0; q < 3; ++q) {
+      if (centroid) centroid[q] = c[q];
+      if (index) index[q] = idx[q];
+    }
+    return TTSH_OK;
+  });
+}
+
+int ttsh_run_dirs(const char* const* dirs, int n, const ttsh_ext* ext, uint64_t seed, int device) {
+  if (!dirs || n <= 0) return set_error(TTSH_E_INVALID, "ttsh_run_dirs: bad arguments");
+  std::vector<ttsh_input> in(n);
+  std::vector<ttsh_ext> ex(n);
+  ttsh_ext d;
+  ttsh_default_ext(&d);
+  for (int i = 0; i < n; ++i) {
+    int rc = ttsh_read_input((std::string(dirs[i]) + "/input.dat").c_str(), &in[i]);
+    if (rc) return rc;
+    ex[i] = ext ? *ext : d;
+  }
+  ttsh_sim* s = nullptr;
+  int rc = ttsh_batch_create(in.data(), ex.data(), n, device, &s);
+  if (rc) return rc;
+  struct Run {
+    double T, Dt, dte, Ts;
+    bool active;
+  };
+  std::vector<Run> run(n);
+  for (int i = 0; i < n; ++i) {
+    const ttsh_input& p = in[i];
+    const size_t nn = (size_t)p.Nx * p.Nx * p.Nx;
+    std::vector<double> phi(nn), P(3 * nn), u(3 * nn), us(3 * nn), Ps(3 * nn);
+    const int t0 = (int)((p.T0 + 0.1 * p.dte) / p.dte);  // TTSH3D.cu:768
+    const std::string conf0 = std::string(dirs[i]) + "/../data/conf_" + std::to_string(t0) + ".dat";
+    rc = ttsh_init_reference(&p, (unsigned)(seed + (uint64_t)i), conf0.c_str(), phi.data(), P.data(), u.data(),
+                             us.data(), Ps.data());
+    if (!rc) rc = ttsh_set_state(s, i, phi.data(), P.data(), u.data(), us.data(), Ps.data());
+    if (!rc && p.T0 == 0) rc = ttsh_write_conf(s, i, (std::string(dirs[i]) + "/conf_0.dat").c_str());
+    if (rc) {
+      ttsh_destroy(s);
+      return rc;
+    }
+    run[i] = {p.T0, p.dt0, p.dte, p.Ts, true};
+  }
+  // evolve() of every droplet in lockstep (TTSH3D.cu:311-331): advance to the nearest event
+  for (;;) {
+    int nact = 0;
+    int k = 1 << 30;
+    for (int i = 0; i < n; ++i) {
+      if (!run[i].active) continue;
+      ++nact;
+      double T = run[i].T;
+      int m = 0;
+      for (;;) {  // steps until this droplet's next snapshot or stop
+        T = T + run[i].Dt;
+        ++m;
+        if (std::floor(T / run[i].dte) > std::floor((T - run[i].Dt) / run[i].dte) || T > run[i].Ts || m >= (1 << 20))
+          break;
+      }
+      k = std::min(k, m);
+    }
+    if (nact == 0) break;
+    if ((rc = ttsh_step(s, k)) != 0) break;
+    for (int i = 0; i < n && !rc; ++i) {
+      if (!run[i].active) {
+        for (int m = 0; m < k; ++m) run[i].T = run[i].T + run[i].Dt;
+        continue;
+      }
+      for (int m = 0; m < k && !rc; ++m) {
+        run[i].T = run[i].T + run[i].Dt;
+        if (m + 1 < k) continue;  // events only happen at the k-th step (k is the minimum distance)
+        if (std::floor(run[i].T / run[i].dte) > std::floor((run[i].T - run[i].Dt) / run[i].dte)) {
+          const long te = (long)std::floor(run[i].T / run[i].dte);
+          rc = ttsh_write_conf(s, i, (std::string(dirs[i]) + "/conf_" + std::to_string(te) + ".dat").c_str());
+        }
+        if (run[i].T > run[i].Ts) run[i].active = false;
+      }
+    }
+    if (rc) break;
+  }
+  ttsh_destroy(s);
+  return rc;
+}
+
+static const char kCkpMagic[8] = {'T', 'T', 'S', 'H', 'C', 'K', 'P', '1'};
+
+int ttsh_save_checkpoint(ttsh_sim* s, int inst, const char* path) {
+  int rc = check_inst(s, inst);
+  if (rc) return rc;
+  if (!path) return set_error(TTSH_E_INVALID, "null path");
+  return guarded([&]() -> int {
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    const int N = s->inst[inst].N;
+    const size_t n = (size_t)N * N * N, es = s->precision == 32 ? 4 : 8;
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) return set_error(TTSH_E_IO, std::string("cannot open ") + path);
+    int32_t hdr[4] = {1, N, s->precision, 0};
+    double T = s->inst[inst].T;
+    int64_t steps = s->steps;
+    bool ok = std::fwrite(kCkpMagic, 1, 8, fp) == 8 && std::fwrite(hdr, 4, 4, fp) == 4 &&
+              std::fwrite(&T, 8, 1, fp) == 1 && std::fwrite(&steps, 8, 1, fp) == 1;
+    std::vector<char> buf(n * es);
+    std::vector<void*> arr;
+    s->with_engine([&](auto& E) { arr = state_arrays(s, E, inst); });
+    for (void* d : arr) {
+      if (!ok) break;
+      CK(cudaMemcpy(buf.data(), d, n * es, cudaMemcpyDeviceToHost));
+      ok = std::fwrite(buf.data(), 1, n * es, fp) == n * es;
+    }
+    if (std::fclose(fp) != 0) ok = false;
+    return ok ? TTSH_OK : set_error(TTSH_E_IO, std::string("write failed: ") + path);
+  });
+}
+
+int ttsh_load_checkpoint(ttsh_sim* s, int inst, const char* path) {
+  int rc = check_inst(s, inst);
+  if (rc) return rc;
+  if (!path) return set_error(TTSH_E_INVALID, "null path");
+  return guarded([&]() -> int {
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    const int N = s->inst[inst].N;
+    const size_t n = (size_t)N * N * N, es = s->precision == 32 ? 4 : 8;
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) return set_error(TTSH_E_IO, std::string("cannot open ") + path);
+    char magic[8];
+    int32_t hdr[4];
+    double T;
+    int64_t steps;
+    bool ok = std::fread(magic, 1, 8, fp) == 8 && std::memcmp(magic, kCkpMagic, 8) == 0 &&
+              std::fread(hdr, 4, 4, fp) == 4 && std::fread(&T, 8, 1, fp) == 1 && std::fread(&steps, 8, 1, fp) == 1;
+    if (!ok || hdr[0] != 1) {
+      std::fclose(fp);
+      return set_error(TTSH_E_PARSE, std::string("not a ttsh checkpoint: ") + path);
+    }
+    if (hdr[1] != N || hdr[2] != s->precision) {
+      std::fclose(fp);
+      return set_error(TTSH_E_INVALID, "checkpoint size or precision differs from the instance");
+    }
+    std::vector<char> buf(n * es);
+    std::vector<void*> arr;
+    s->with_engine([&](auto& E) { arr = state_arrays(s, E, inst); });
+    for (void* d : arr) {
+      if (std::fread(buf.data(), 1, n * es, fp) != n * es) {
+        std::fclose(fp);
+        return set_error(TTSH_E_PARSE, std::string("truncated checkpoint: ") + path);
+      }
+      CK(cudaMemcpy(d, buf.data(), n * es, cudaMemcpyHostToDevice));
+    }
+    std::fclose(fp);
+    s->inst[inst].T = T;
+    return TTSH_OK;
+  });
 }
 
 int ttsh_profile_kernels(ttsh_sim* s, int nsteps, int cap, const char** names, double* ms_per_step,

@@ -16,9 +16,13 @@
 #include <stdexcept>
 
 #include "common.cuh"
+#include "fftreg.cuh"
 #include "kernels.h"
 
 namespace ttsh {
+
+using fftreg::poisson_mul;
+using fftreg::scale_n3;
 
 namespace {
 
@@ -104,43 +108,6 @@ __device__ C* run_fft(C* a, C* b, int N, int LB, int pitch, const int* radix, in
     Ns *= R;
   }
   return a;
-}
-
-// -F / k^2 of getStream mode 1 (:672-683) with k2 from initPoissonSolver (:1088-1124).
-__device__ __forceinline__ double2 poisson_mul(double2 v, const InstDev<double>& I, int x, int y, int z) {
-  double k2;
-  if (I.k2mode == 0) {
-    const double kx = I.kval[x], ky = I.kval[y], kz = I.kval[z];
-    // the host's kx*kx + ky*ky + kz*kz, without contraction
-    k2 = __dadd_rn(__dadd_rn(__dmul_rn(kx, kx), __dmul_rn(ky, ky)), __dmul_rn(kz, kz));
-    if ((x | y | z) == 0) k2 = 1;  // k2[0] = 1 (:1120)
-  } else {
-    const double Kx = I.St[x] * I.Ct[y] * I.Ct[z], Ky = I.Ct[x] * I.St[y] * I.Ct[z], Kz = I.Ct[x] * I.Ct[y] * I.St[z];
-    k2 = Kx * Kx + Ky * Ky + Kz * Kz;
-    if (k2 < 1e-8 / ((double)I.ph.h * (double)I.ph.h)) return make_double2(0.0, 0.0);
-  }
-  return make_double2(-v.x / k2, -v.y / k2);
-}
-__device__ __forceinline__ float2 poisson_mul(float2 v, const InstDev<float>& I, int x, int y, int z) {
-  float k2;
-  if (I.k2mode == 0) {
-    k2 = I.k2t[x] + I.k2t[y] + I.k2t[z];
-    if ((x | y | z) == 0) k2 = 1.f;
-  } else {
-    const float Kx = I.St[x] * I.Ct[y] * I.Ct[z], Ky = I.Ct[x] * I.St[y] * I.Ct[z], Kz = I.Ct[x] * I.Ct[y] * I.St[z];
-    k2 = Kx * Kx + Ky * Ky + Kz * Kz;
-    if (k2 < 1e-8f / (I.ph.h * I.ph.h)) return make_float2(0.f, 0.f);
-  }
-  const float f = -1.f / k2;
-  return make_float2(v.x * f, v.y * f);
-}
-
-__device__ __forceinline__ double2 scale_n3(double2 v, const InstDev<double>& I) {
-  const double n3 = (double)(I.N * I.N * I.N);
-  return make_double2(v.x / n3, v.y / n3);
-}
-__device__ __forceinline__ float2 scale_n3(float2 v, const InstDev<float>& I) {
-  return make_float2(v.x * I.ph.invN3, v.y * I.ph.invN3);
 }
 
 template <class T, int PASS>
@@ -230,6 +197,7 @@ void set_attr(int N) {
 
 template <class T>
 void fft_prepare(int N) {
+  fftreg_prepare<T>(N);
   set_attr<T, 0>(N);
   set_attr<T, 1>(N);
   set_attr<T, 2>(N);
@@ -245,6 +213,7 @@ size_t fft_smem_bytes(int N, int) {
 
 template <class T>
 void launch_fft_pass(const Group<T>& g, int pass, cudaStream_t st) {
+  if (fftreg_launch<T>(g, pass, st)) return;
   switch (pass) {
     case 0: launch_one<T, 0>(g, st); break;
     case 1: launch_one<T, 1>(g, st); break;

@@ -1,0 +1,15 @@
+// fftreg_f32.cu — register-resident FFT passes instantiated for float (see fftreg_impl.cuh).
+#include "fftreg_impl.cuh"
+
+namespace ttsh {
+
+template <>
+bool fftreg_launch<float>(const Group<float>& g, int pass, cudaStream_t st) {
+  return g.fft_kind == 0 && fftreg::reg_launch<float>(g, pass, st);
+}
+template <>
+void fftreg_prepare<float>(int N) {
+  fftreg::reg_prepare<float>(N);
+}
+
+}  // namespace ttsh

@@ -1,0 +1,15 @@
+// fftreg_f64.cu — register-resident FFT passes instantiated for double (see fftreg_impl.cuh).
+#include "fftreg_impl.cuh"
+
+namespace ttsh {
+
+template <>
+bool fftreg_launch<double>(const Group<double>& g, int pass, cudaStream_t st) {
+  return g.fft_kind == 0 && fftreg::reg_launch<double>(g, pass, st);
+}
+template <>
+void fftreg_prepare<double>(int N) {
+  fftreg::reg_prepare<double>(N);
+}
+
+}  // namespace ttsh

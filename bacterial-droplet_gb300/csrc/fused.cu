@@ -1,4 +1,26 @@
-// fused.cu — fused FP32 form of the step (filled in once the plain form is parity-checked).
+// fused.cu — the fused FP32 form of the TTSH3D step.
+//
+// Three kernels replace stage1 + stage2 + div + correct of the plain form (plain.cu):
+//
+//   fused_rhs     phi, P, u -> u*, P*, phi'   (getTempVari_1/2 + getDtF + getVStar + the phi
+//                 update of getVNew, TTSH3D.cu:537-632, :471-491, :515), all intermediates
+//                 (mu_0, mu_b, the stress S_ab, D_a P_b) kept in shared memory.
+//   fused_div     u*, P* -> W = div(u*)/dt + i div(P*)/dt   (getStream mode 0, :664-670, with
+//                 the reference's stale halo for neighbours across the periodic boundary)
+//   fused_correct u*, P*, W -> u, P   (getVNew, :505-511)
+//
+// All three march along z through a tile of TX x TY columns (a "2.5D" sweep): each z-plane of
+// every field the stencils need is staged once in a shared-memory ring of planes, and each
+// thread evaluates the 27-point derivatives / 15-point Laplacians of a 1 x RY strip of sites
+// from registers (the strip's 3 x (RY+2) x 3 neighbourhood), so warps read shared memory with
+// unit stride. The nested stencils of the RHS (sigma and mu need D P and L P; the velocity
+// update needs D sigma and L mu) are staged: the ring of stage-1 products at plane z+1 is built
+// one plane ahead of the plane z whose update reads it.
+//
+// The stencil arithmetic is the reference's (st_dx/st_dy/st_dz/st_lap of common.cuh) in FP32;
+// the stress enters as one field per component, S_ab = cA phi D_a P_b - zeta phi P_a P_b, whose
+// divergence is the reference's cA * div(sigma) plus the build-defined active stress.
+#include <cstdio>
 #include <stdexcept>
 
 #include "common.cuh"
@@ -6,8 +28,493 @@
 
 namespace ttsh {
 
-bool fused_supported(int) { return false; }
-void launch_fused_rhs(const Group<float>&, int, cudaStream_t) { throw std::runtime_error("fused form not built"); }
-void launch_fused_correct(const Group<float>&, int, cudaStream_t) { throw std::runtime_error("fused form not built"); }
+namespace {
+
+constexpr int TX = 32, TY = 16;   // output tile (columns)
+constexpr int ZC = 64;            // z-planes per block (chunk)
+constexpr int RY = 2;             // strip length (sites per thread) in fused_rhs
+constexpr int NT = 256;           // threads of fused_rhs
+
+// fused_rhs regions: A = tile + 2 (phi, P), B = tile + 1 (u, stage-1 products), C = tile.
+constexpr int AW = TX + 4, AH = TY + 4, AN = AW * AH;
+constexpr int BW = TX + 2, BH = TY + 2, BN = BW * BH;
+constexpr int CN = TX * TY;
+// shared memory (floats): A ring 5 planes x 4 fields; u ring 4 x 3; B ring 3 x 13; D P ring 2 x 9.
+// The A and u rings hold one plane more than the stencils read: the next plane is copied into
+// it (cp.async) while the current planes are being computed.
+constexpr int RA = 5, RU = 4;
+constexpr int SA_OFF = 0;
+constexpr int SU_OFF = SA_OFF + RA * 4 * AN;
+constexpr int SB_OFF = SU_OFF + RU * 3 * BN;
+constexpr int SD_OFF = SB_OFF + 3 * 13 * BN;
+constexpr int RHS_SMEM_FLOATS = SD_OFF + 2 * 9 * CN;
+constexpr size_t RHS_SMEM = RHS_SMEM_FLOATS * sizeof(float);
+// stage-1 product slots in the B ring
+constexpr int QS = 0, QMU = 9, QMU0 = 12, NQ = 13;
+
+__device__ __forceinline__ int wrapN(int a, int N) { return a < 0 ? a + N : (a >= N ? a - N : a); }
+
+// Asynchronous global -> shared copies (cp.async): the data lands while the CTA computes.
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// A 3 (planes) x (R+2) (rows) x 3 (columns) neighbourhood held in registers, for a strip of R
+// sites stacked in y. F(dx,dy,dz) of site k reads v[1+dz][1+k+dy][1+dx].
+template <int R>
+struct Hood {
+  float v[3][R + 2][3];
+  __device__ __forceinline__ void load(const float* p0, const float* p1, const float* p2, int W, int x, int y0) {
+    const float* pl[3] = {p0, p1, p2};
+#pragma unroll
+    for (int z = 0; z < 3; ++z)
+#pragma unroll
+      for (int r = 0; r < R + 2; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) v[z][r][c] = pl[z][(y0 - 1 + r) * W + (x - 1 + c)];
+  }
+};
+template <int R>
+struct HoodAcc {
+  const Hood<R>* h;
+  int k;
+  __device__ __forceinline__ float operator()(int dx, int dy, int dz) const { return h->v[1 + dz][1 + k + dy][1 + dx]; }
+};
+
+// Interleaved-complex variant (one component of a float2 plane).
+template <int R>
+struct Hood2 {
+  float2 v[3][R + 2][3];
+  __device__ __forceinline__ void load(const float2* p0, const float2* p1, const float2* p2, int W, int x, int y0) {
+    const float2* pl[3] = {p0, p1, p2};
+#pragma unroll
+    for (int z = 0; z < 3; ++z)
+#pragma unroll
+      for (int r = 0; r < R + 2; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) v[z][r][c] = pl[z][(y0 - 1 + r) * W + (x - 1 + c)];
+  }
+};
+template <int R, int COMP>
+struct Hood2Acc {
+  const Hood2<R>* h;
+  int k;
+  __device__ __forceinline__ float operator()(int dx, int dy, int dz) const {
+    const float2 t = h->v[1 + dz][1 + k + dy][1 + dx];
+    return COMP == 0 ? t.x : t.y;
+  }
+};
+
+// ------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __restrict__ insts, int par, int nchunk) {
+  extern __shared__ __align__(16) float sm[];
+  const int N = insts[0].N;
+  const InstDev<float>& I = insts[blockIdx.z / nchunk];
+  const Phys<float>& p = I.ph;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+  const int z0 = (blockIdx.z % nchunk) * ZC;
+  const int z1 = min(z0 + ZC, N);
+  const size_t NN = (size_t)N * N;
+  const float* __restrict__ gphi = I.phi[par];
+  const float* __restrict__ gP[3] = {I.P[0], I.P[1], I.P[2]};
+  const float* __restrict__ gU[3] = {I.U[0], I.U[1], I.U[2]};
+  float* sA = sm + SA_OFF;  // [slot 4][field 4][AN]
+  float* sU = sm + SU_OFF;  // [slot 3][comp 3][BN]
+  float* sB = sm + SB_OFF;  // [slot 3][q 13][BN]
+  float* sD = sm + SD_OFF;  // [slot 2][9][CN]
+  const int tid = threadIdx.x;
+  const int niter = (z1 - z0) + 4;
+
+  // Stage 0 of iteration i: A plane a = z0 - 2 + i (phi, P over tile+2) into A slot i % RA and,
+  // from i = 2 on, u plane a - 1 (tile+1) into u slot i % RU. Issued one iteration ahead.
+  auto issue = [&](int i) {
+    const int za = ((z0 - 2 + i) % N + N) % N;
+    float* dst = sA + (i % RA) * 4 * AN;
+    for (int t = tid; t < AN; t += NT) {
+      const int ay = t / AW, ax = t - ay * AW;
+      const size_t g = (size_t)za * NN + (size_t)wrapN(y0 - 2 + ay, N) * N + wrapN(x0 - 2 + ax, N);
+      cp_async4(dst + t, gphi + g);
+      cp_async4(dst + AN + t, gP[0] + g);
+      cp_async4(dst + 2 * AN + t, gP[1] + g);
+      cp_async4(dst + 3 * AN + t, gP[2] + g);
+    }
+    if (i >= 2) {
+      const int zu = ((z0 - 3 + i) % N + N) % N;
+      float* du = sU + (i % RU) * 3 * BN;
+      for (int t = tid; t < BN; t += NT) {
+        const int by = t / BW, bx = t - by * BW;
+        const size_t g = (size_t)zu * NN + (size_t)wrapN(y0 - 1 + by, N) * N + wrapN(x0 - 1 + bx, N);
+        cp_async4(du + t, gU[0] + g);
+        cp_async4(du + BN + t, gU[1] + g);
+        cp_async4(du + 2 * BN + t, gU[2] + g);
+      }
+    }
+    cp_async_commit();
+  };
+  issue(0);
+  for (int i = 0; i < niter; ++i) {
+    cp_async_wait_all();
+    __syncthreads();
+    if (i + 1 < niter) issue(i + 1);
+    // ---- stage 1 at plane b = z0 - 3 + i over B (tile+1): mu_0, mu_b, S_ab (+ D P on the tile)
+    if (i >= 2) {
+      const float* a0 = sA + ((i + RA - 2) % RA) * 4 * AN;  // plane b-1
+      const float* a1 = sA + ((i + RA - 1) % RA) * 4 * AN;  // plane b
+      const float* a2 = sA + (i % RA) * 4 * AN;             // plane b+1
+      float* bq = sB + (i % 3) * NQ * BN;
+      float* dq = sD + (i & 1) * 9 * CN;
+      for (int s = tid; s < BW * (BH / RY); s += NT) {
+        const int bx = s % BW, by0 = (s / BW) * RY;
+        const int ax = bx + 1, ay0 = by0 + 1;  // in A coordinates
+        float phc[RY], lphi[RY];
+        {
+          Hood<RY> h;
+          h.load(a0, a1, a2, AW, ax, ay0);
+#pragma unroll
+          for (int k = 0; k < RY; ++k) {
+            HoodAcc<RY> F{&h, k};
+            phc[k] = F(0, 0, 0);
+            lphi[k] = st_lap<float>(F, p);
+          }
+        }
+        float Pc[3][RY], DP[3][3][RY];  // DP[a][b] = D_a P_b
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+          Hood<RY> h;
+          h.load(a0 + (1 + b) * AN, a1 + (1 + b) * AN, a2 + (1 + b) * AN, AW, ax, ay0);
+#pragma unroll
+          for (int k = 0; k < RY; ++k) {
+            HoodAcc<RY> F{&h, k};
+            Pc[b][k] = F(0, 0, 0);
+            DP[0][b][k] = st_dx<float>(F, p.c2h);
+            DP[1][b][k] = st_dy<float>(F, p.c2h);
+            DP[2][b][k] = st_dz<float>(F, p.c2h);
+            const float lp = st_lap<float>(F, p);
+            bq[(QMU + b) * BN + (by0 + k) * BW + bx] = phc[k] * Pc[b][k] + p.La2 * lp;  // mu_b (:571-573)
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < RY; ++k) {
+          const float ph = phc[k];
+          const int o = (by0 + k) * BW + bx;
+          bq[QMU0 * BN + o] = p.aPhi2 * (ph - 3 * ph * ph + 2 * ph * ph * ph) - p.kPhi * lphi[k];  // mu_0 (:567)
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+              float sv = p.cA * (ph * DP[a][b][k]);  // cA * sigma_ab (:587-595)
+              if (p.zeta != 0.f) sv -= p.zeta * (ph * Pc[a][k] * Pc[b][k]);
+              bq[(QS + a * 3 + b) * BN + o] = sv;
+            }
+          const int cx = bx - 1, cy = by0 + k - 1;
+          if (cx >= 0 && cx < TX && cy >= 0 && cy < TY) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+              for (int b = 0; b < 3; ++b) dq[(a * 3 + b) * CN + cy * TX + cx] = DP[a][b][k];
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // ---- stage 2 at plane c = z0 - 4 + i over the tile: d/dt u, P, phi -> u*, P*, phi'
+    if (i >= 4) {
+      const int zc = z0 - 4 + i;  // in [z0, z1)
+      const float* a0 = sA + ((i + RA - 3) % RA) * 4 * AN;  // plane c-1
+      const float* a1 = sA + ((i + RA - 2) % RA) * 4 * AN;  // plane c
+      const float* a2 = sA + ((i + RA - 1) % RA) * 4 * AN;  // plane c+1
+      const float* u0 = sU + ((i + RU - 2) % RU) * 3 * BN;
+      const float* u1 = sU + ((i + RU - 1) % RU) * 3 * BN;
+      const float* u2 = sU + (i % RU) * 3 * BN;
+      const float* q0 = sB + ((i + 1) % 3) * NQ * BN;
+      const float* q1 = sB + ((i + 2) % 3) * NQ * BN;
+      const float* q2 = sB + (i % 3) * NQ * BN;
+      const float* dq = sD + ((i + 1) & 1) * 9 * CN;
+      for (int s = tid; s < TX * (TY / RY); s += NT) {
+        const int cx = s % TX, cy0 = (s / TX) * RY;
+        const int bx = cx + 1, by0 = cy0 + 1, ax = cx + 2, ay0 = cy0 + 2;
+        float phc[RY], dphi[3][RY];
+        {
+          Hood<RY> h;
+          h.load(a0, a1, a2, AW, ax, ay0);
+#pragma unroll
+          for (int k = 0; k < RY; ++k) {
+            HoodAcc<RY> F{&h, k};
+            phc[k] = F(0, 0, 0);
+            dphi[0][k] = st_dx<float>(F, p.c2h);
+            dphi[1][k] = st_dy<float>(F, p.c2h);
+            dphi[2][k] = st_dz<float>(F, p.c2h);
+          }
+        }
+        float uc[3][RY], du[3][3][RY], lu[3][RY];  // du[b][a] = D_a u_b
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+          Hood<RY> h;
+          h.load(u0 + b * BN, u1 + b * BN, u2 + b * BN, BW, bx, by0);
+#pragma unroll
+          for (int k = 0; k < RY; ++k) {
+            HoodAcc<RY> F{&h, k};
+            uc[b][k] = F(0, 0, 0);
+            du[b][0][k] = st_dx<float>(F, p.c2h);
+            du[b][1][k] = st_dy<float>(F, p.c2h);
+            du[b][2][k] = st_dz<float>(F, p.c2h);
+            lu[b][k] = st_lap<float>(F, p);
+          }
+        }
+        float mu0c[RY], lmu0[RY];
+        {
+          Hood<RY> h;
+          h.load(q0 + QMU0 * BN, q1 + QMU0 * BN, q2 + QMU0 * BN, BW, bx, by0);
+#pragma unroll
+          for (int k = 0; k < RY; ++k) {
+            HoodAcc<RY> F{&h, k};
+            mu0c[k] = F(0, 0, 0);
+            lmu0[k] = st_lap<float>(F, p);
+          }
+        }
+        // velocity: d/dt u_b (:617-621) + the stress divergence; u*_b = u_b + dt d/dt u_b (:480-482)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+          float fdiv[RY];
+          {
+            Hood<RY> hx, hy, hz;
+            hx.load(q0 + (QS + 0 * 3 + b) * BN, q1 + (QS + 0 * 3 + b) * BN, q2 + (QS + 0 * 3 + b) * BN, BW, bx, by0);
+            hy.load(q0 + (QS + 1 * 3 + b) * BN, q1 + (QS + 1 * 3 + b) * BN, q2 + (QS + 1 * 3 + b) * BN, BW, bx, by0);
+            hz.load(q0 + (QS + 2 * 3 + b) * BN, q1 + (QS + 2 * 3 + b) * BN, q2 + (QS + 2 * 3 + b) * BN, BW, bx, by0);
+#pragma unroll
+            for (int k = 0; k < RY; ++k)
+              fdiv[k] = st_dx<float>(HoodAcc<RY>{&hx, k}, p.c2h) + st_dy<float>(HoodAcc<RY>{&hy, k}, p.c2h) +
+                        st_dz<float>(HoodAcc<RY>{&hz, k}, p.c2h);
+          }
+#pragma unroll
+          for (int k = 0; k < RY; ++k) {
+            const float r = -uc[0][k] * du[b][0][k] - uc[1][k] * du[b][1][k] - uc[2][k] * du[b][2][k] +
+                            p.mu * lu[b][k] + mu0c[k] * dphi[b][k] + fdiv[k];
+            const size_t g = (size_t)zc * NN + (size_t)(y0 + cy0 + k) * N + (x0 + cx);
+            I.Us[par ^ 1][b][g] = uc[b][k] + p.dt * r;
+          }
+        }
+        // polarisation: d/dt P_b (:623-629); P*_b = P_b + dt d/dt P_b (:486-488)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+          Hood<RY> h;
+          h.load(q0 + (QMU + b) * BN, q1 + (QMU + b) * BN, q2 + (QMU + b) * BN, BW, bx, by0);
+#pragma unroll
+          for (int k = 0; k < RY; ++k) {
+            const int c = (cy0 + k) * TX + cx;
+            const float px = a1[1 * AN + (ay0 + k) * AW + ax], py = a1[2 * AN + (ay0 + k) * AW + ax],
+                        pz = a1[3 * AN + (ay0 + k) * AW + ax];
+            const float pb = b == 0 ? px : (b == 1 ? py : pz);
+            const float dxp = dq[(0 * 3 + b) * CN + c], dyp = dq[(1 * 3 + b) * CN + c], dzp = dq[(2 * 3 + b) * CN + c];
+            const float P2 = px * px + py * py + pz * pz;
+            const float dPhi2 = dphi[0][k] * dphi[0][k] + dphi[1][k] * dphi[1][k] + dphi[2][k] * dphi[2][k];
+            float cub;
+            if (b == 0) cub = px * px * px + px * py * py + px * pz * pz;
+            else if (b == 1) cub = px * py * px + py * py * py + py * pz * pz;
+            else cub = px * pz * px + py * pz * py + pz * pz * pz;
+            const float Ab = dphi[0][k] * dphi[b][k] * px + dphi[1][k] * dphi[b][k] * py + dphi[2][k] * dphi[b][k] * pz;
+            const float r = -uc[0][k] * dxp - uc[1][k] * dyp - uc[2][k] * dzp - p.alpha * phc[k] * pb -
+                            p.beta * P2 * pb + p.eta * st_lap<float>(HoodAcc<RY>{&h, k}, p) -
+                            p.lambda0 * (px * dxp + py * dyp + pz * dzp) - p.A * (dPhi2 * cub + sqrtf(P2) * Ab);
+            const size_t g = (size_t)zc * NN + (size_t)(y0 + cy0 + k) * N + (x0 + cx);
+            I.Ps[par ^ 1][b][g] = pb + p.dt * r;
+          }
+        }
+        // phi: d/dt phi (:631), phi' = phi + dt d/dt phi (:515)
+#pragma unroll
+        for (int k = 0; k < RY; ++k) {
+          const float dtphi = -uc[0][k] * dphi[0][k] - uc[1][k] * dphi[1][k] - uc[2][k] * dphi[2][k] + p.gamma * lmu0[k];
+          const size_t g = (size_t)zc * NN + (size_t)(y0 + cy0 + k) * N + (x0 + cx);
+          I.phi[par ^ 1][g] = phc[k] + p.dt * dtphi;
+        }
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// fused_div / fused_correct: one ring of 3 planes over tile+1, strips of RD sites.
+constexpr int RD = 4;
+constexpr int NTD = TX * TY / RD;  // 128 threads
+constexpr int DN = (TX + 2) * (TY + 2);
+constexpr int RR = 4;  // ring planes of fused_div / fused_correct (3 read + 1 in flight)
+constexpr size_t DIV_SMEM = RR * 6 * DN * sizeof(float);
+constexpr size_t COR_SMEM = RR * DN * sizeof(float2) + 3 * 6 * TX * TY * sizeof(float);
+
+__global__ void __launch_bounds__(NTD) k_fused_div(const InstDev<float>* __restrict__ insts, int par, int nchunk) {
+  extern __shared__ __align__(16) float sm[];
+  const int N = insts[0].N;
+  const InstDev<float>& I = insts[blockIdx.z / nchunk];
+  const Phys<float>& p = I.ph;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+  const int z0 = (blockIdx.z % nchunk) * ZC, z1 = min(z0 + ZC, N);
+  const size_t NN = (size_t)N * N;
+  const float* cur[6] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2],
+                         I.Ps[par ^ 1][0], I.Ps[par ^ 1][1], I.Ps[par ^ 1][2]};
+  const float* old[6] = {I.Us[par][0], I.Us[par][1], I.Us[par][2], I.Ps[par][0], I.Ps[par][1], I.Ps[par][2]};
+  const int W = TX + 2;
+  const int niter = (z1 - z0) + 2;
+  // plane z0 - 1 + i into slot i % RR, issued one iteration ahead
+  auto issue = [&](int i) {
+    const int zu = z0 - 1 + i;
+    const bool zw = zu < 0 || zu >= N;
+    const int zz = wrapN(zu, N);
+    float* dst = sm + (i % RR) * 6 * DN;
+    for (int t = threadIdx.x; t < DN; t += NTD) {
+      const int ry = t / W, rx = t - ry * W;
+      const int gx = x0 - 1 + rx, gy = y0 - 1 + ry;
+      const bool stale = I.stale && (zw || gx < 0 || gx >= N || gy < 0 || gy >= N);
+      const size_t g = (size_t)zz * NN + (size_t)wrapN(gy, N) * N + wrapN(gx, N);
+#pragma unroll
+      for (int f = 0; f < 6; ++f) cp_async4(dst + f * DN + t, (stale ? old[f] : cur[f]) + g);
+    }
+    cp_async_commit();
+  };
+  issue(0);
+  for (int i = 0; i < niter; ++i) {
+    cp_async_wait_all();
+    __syncthreads();
+    if (i + 1 < niter) issue(i + 1);
+    if (i >= 2) {
+      const int zc = z0 - 2 + i;
+      const float* s0 = sm + ((i + RR - 2) % RR) * 6 * DN;
+      const float* s1 = sm + ((i + RR - 1) % RR) * 6 * DN;
+      const float* s2 = sm + (i % RR) * 6 * DN;
+      const int cx = threadIdx.x % TX, cy0 = (threadIdx.x / TX) * RD;
+      float d[2][RD];
+#pragma unroll
+      for (int f = 0; f < 2; ++f) {
+        Hood<RD> hx, hy, hz;
+        hx.load(s0 + (3 * f + 0) * DN, s1 + (3 * f + 0) * DN, s2 + (3 * f + 0) * DN, W, cx + 1, cy0 + 1);
+        hy.load(s0 + (3 * f + 1) * DN, s1 + (3 * f + 1) * DN, s2 + (3 * f + 1) * DN, W, cx + 1, cy0 + 1);
+        hz.load(s0 + (3 * f + 2) * DN, s1 + (3 * f + 2) * DN, s2 + (3 * f + 2) * DN, W, cx + 1, cy0 + 1);
+#pragma unroll
+        for (int k = 0; k < RD; ++k)
+          d[f][k] = (st_dx<float>(HoodAcc<RD>{&hx, k}, p.c2h) + st_dy<float>(HoodAcc<RD>{&hy, k}, p.c2h) +
+                     st_dz<float>(HoodAcc<RD>{&hz, k}, p.c2h)) * p.inv_dt;
+      }
+#pragma unroll
+      for (int k = 0; k < RD; ++k) {
+        const size_t g = (size_t)zc * NN + (size_t)(y0 + cy0 + k) * N + (x0 + cx);
+        I.W[g] = make_float2(d[0][k], d[1][k]);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(NTD) k_fused_correct(const InstDev<float>* __restrict__ insts, int par, int nchunk) {
+  extern __shared__ __align__(16) float2 sm2[];
+  float* sq = reinterpret_cast<float*>(sm2 + RR * DN);  // [3][6][TX*TY]: u*, P* of the compute planes
+  const int N = insts[0].N;
+  const InstDev<float>& I = insts[blockIdx.z / nchunk];
+  const Phys<float>& p = I.ph;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+  const int z0 = (blockIdx.z % nchunk) * ZC, z1 = min(z0 + ZC, N);
+  const size_t NN = (size_t)N * N;
+  const int W = TX + 2;
+  const int niter = (z1 - z0) + 2;
+  const float* qs[6] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2],
+                        I.Ps[par ^ 1][0], I.Ps[par ^ 1][1], I.Ps[par ^ 1][2]};
+  // issue(i): W plane z0 - 1 + i into ring slot i % RR, and u*, P* of plane z0 - 1 + i (computed at
+  // iteration i + 1) into slot i % 3. issue(i + 1) runs during iteration i, while iteration i reads
+  // the u*, P* slot (i - 1) % 3 and issue(i) has filled slot i % 3.
+  auto issue = [&](int i) {
+    const int zz = ((z0 - 1 + i) % N + N) % N;
+    float2* dst = sm2 + (i % RR) * DN;
+    for (int t = threadIdx.x; t < DN; t += NTD) {
+      const int ry = t / W, rx = t - ry * W;
+      cp_async8(dst + t, I.W + (size_t)zz * NN + (size_t)wrapN(y0 - 1 + ry, N) * N + wrapN(x0 - 1 + rx, N));
+    }
+    const int zq = z0 - 1 + i;
+    if (zq >= z0 && zq < z1) {
+      float* dq = sq + (i % 3) * 6 * TX * TY;
+      for (int t = threadIdx.x; t < TX * TY; t += NTD) {
+        const int cy = t / TX, cx = t - cy * TX;
+        const size_t g = (size_t)zq * NN + (size_t)(y0 + cy) * N + (x0 + cx);
+#pragma unroll
+        for (int f = 0; f < 6; ++f) cp_async4(dq + f * TX * TY + t, qs[f] + g);
+      }
+    }
+    cp_async_commit();
+  };
+  issue(0);
+  for (int i = 0; i < niter; ++i) {
+    cp_async_wait_all();
+    __syncthreads();
+    if (i + 1 < niter) issue(i + 1);
+    if (i >= 2) {
+      const int zc = z0 - 2 + i;
+      const int cx = threadIdx.x % TX, cy0 = (threadIdx.x / TX) * RD;
+      const float* dq = sq + ((i + 2) % 3) * 6 * TX * TY;  // staged by issue(i - 1)
+      Hood2<RD> h;
+      h.load(sm2 + ((i + RR - 2) % RR) * DN, sm2 + ((i + RR - 1) % RR) * DN, sm2 + (i % RR) * DN, W, cx + 1, cy0 + 1);
+#pragma unroll
+      for (int k = 0; k < RD; ++k) {
+        Hood2Acc<RD, 0> Fv{&h, k};
+        Hood2Acc<RD, 1> Fp{&h, k};
+        const int c = (cy0 + k) * TX + cx;
+        const size_t g = (size_t)zc * NN + (size_t)(y0 + cy0 + k) * N + (x0 + cx);
+        // getVNew (TTSH3D.cu:505-511)
+        I.U[0][g] = dq[0 * TX * TY + c] - p.dt * st_dx<float>(Fv, p.c2h);
+        I.U[1][g] = dq[1 * TX * TY + c] - p.dt * st_dy<float>(Fv, p.c2h);
+        I.U[2][g] = dq[2 * TX * TY + c] - p.dt * st_dz<float>(Fv, p.c2h);
+        I.P[0][g] = dq[3 * TX * TY + c] - p.dt * st_dx<float>(Fp, p.c2h);
+        I.P[1][g] = dq[4 * TX * TY + c] - p.dt * st_dy<float>(Fp, p.c2h);
+        I.P[2][g] = dq[5 * TX * TY + c] - p.dt * st_dz<float>(Fp, p.c2h);
+      }
+    }
+  }
+}
+
+inline void check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+dim3 grid_for(const Group<float>& g, int& nchunk) {
+  nchunk = (g.N + ZC - 1) / ZC;
+  if ((long)nchunk * g.n > 65535) throw std::runtime_error("fused: too many droplets in one group");
+  return dim3(g.N / TX, g.N / TY, nchunk * g.n);
+}
+
+}  // namespace
+
+bool fused_supported(int N) { return N >= 32 && N % TX == 0 && N % TY == 0; }
+
+void fused_prepare() {
+  check(cudaFuncSetAttribute(k_fused_rhs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RHS_SMEM),
+        "fused_rhs smem attribute");
+  check(cudaFuncSetAttribute(k_fused_div, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DIV_SMEM),
+        "fused_div smem attribute");
+  check(cudaFuncSetAttribute(k_fused_correct, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)COR_SMEM),
+        "fused_correct smem attribute");
+}
+
+void launch_fused_rhs(const Group<float>& g, int par, cudaStream_t st) {
+  int nchunk;
+  dim3 grid = grid_for(g, nchunk);
+  k_fused_rhs<<<grid, NT, RHS_SMEM, st>>>(g.d_inst, par, nchunk);
+  check(cudaGetLastError(), "fused_rhs launch");
+}
+
+void launch_fused_div(const Group<float>& g, int par, cudaStream_t st) {
+  int nchunk;
+  dim3 grid = grid_for(g, nchunk);
+  k_fused_div<<<grid, NTD, DIV_SMEM, st>>>(g.d_inst, par, nchunk);
+  check(cudaGetLastError(), "fused_div launch");
+}
+
+void launch_fused_correct(const Group<float>& g, int par, cudaStream_t st) {
+  int nchunk;
+  dim3 grid = grid_for(g, nchunk);
+  k_fused_correct<<<grid, NTD, COR_SMEM, st>>>(g.d_inst, par, nchunk);
+  check(cudaGetLastError(), "fused_correct launch");
+}
 
 }  // namespace ttsh

@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <random>
 #include <string>
 #include <thread>
 #include <vector>
@@ -117,6 +118,42 @@ int ttsh_format_conf(int N, int expo_data, const double* phi, const double* P, c
   }
   if (std::fclose(fp) != 0) err = 1;
   if (err) return set_error(TTSH_E_IO, std::string("write failed: ") + path);
+  return TTSH_OK;
+}
+
+int ttsh_init_reference(const ttsh_input* in, unsigned seed, const char* conf0_path, double* phi, double* P,
+                        double* u, double* ustar, double* Pstar) {
+  if (!in || !phi || !P || !u || !ustar || !Pstar) return set_error(TTSH_E_INVALID, "ttsh_init_reference: null");
+  const int N = in->Nx;
+  if (N <= 0 || in->Ny != N || in->Nz != N) return set_error(TTSH_E_INVALID, "ttsh_init_reference: grid");
+  const size_t n = (size_t)N * N * N;
+  std::fill(phi, phi + n, 0.0);
+  std::fill(P, P + 3 * n, 0.0);
+  std::fill(u, u + 3 * n, 0.0);
+  std::fill(ustar, ustar + 3 * n, 0.0);
+  std::fill(Pstar, Pstar + 3 * n, 0.0);
+  std::default_random_engine rng(seed);
+  std::uniform_real_distribution<double> randUR;
+  std::ifstream conf;
+  if (in->InitCond == 0 && conf0_path) conf.open(conf0_path);
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < N; j++)
+      for (int k = 0; k < N; k++) {
+        const size_t idx = ((size_t)k * N + j) * N + i;  // x = i, y = j, z = k (TTSH3D.cu:786-791)
+        if (in->InitCond == 0) {
+          conf >> u[idx] >> u[n + idx];
+        } else if (in->InitCond == 1) {
+          double* tgt[12] = {&u[idx], &u[n + idx], &u[2 * n + idx], &ustar[idx], &ustar[n + idx],
+                             &ustar[2 * n + idx], &P[idx], &P[n + idx], &P[2 * n + idx], &Pstar[idx],
+                             &Pstar[n + idx], &Pstar[2 * n + idx]};
+          for (int c = 0; c < 12; ++c) *tgt[c] = 0 + in->init0 * (randUR(rng) - 0.5);
+          const double dx = (i - in->Nx / 2.), dy = (j - in->Ny / 2.), dz = (k - in->Nz / 2.);
+          const double r = std::sqrt(dx * dx + dy * dy + dz * dz);
+          phi[idx] = (1 - std::tanh((r - in->Nx / 4.) * 2)) / 2;
+          (void)randUR(rng);  // p_v (recomputed by the first projection)
+          (void)randUR(rng);  // p_p
+        }
+      }
   return TTSH_OK;
 }
 

@@ -12,6 +12,7 @@ struct Group {
   InstDev<T>* d_inst;  // device array [n]
   int n;               // instances in the group
   int N;
+  int fft_kind = 0;    // 0: register-resident FFT kernels where the size has them; 1: Stockham only
 };
 
 // Plain form (one thread per site, reference arithmetic order), plain.cu.
@@ -29,10 +30,23 @@ template <class T> void launch_fft_pass(const Group<T>& g, int pass, cudaStream_
 template <class T> size_t fft_smem_bytes(int N, int pass);
 // Sets the dynamic shared-memory limits of the FFT kernels for size N (call before capture).
 template <class T> void fft_prepare(int N);
+// Register-resident FFT passes (fftreg_*.cu): false when the size has none (Stockham is used).
+template <class T> bool fftreg_launch(const Group<T>& g, int pass, cudaStream_t st);
+template <class T> void fftreg_prepare(int N);
 
-// Fused FP32 form (fused.cu).
+// Fused FP32 form (fused.cu): rhs (u*, P*, phi'), div (packed Poisson source), correct (u, P).
 void launch_fused_rhs(const Group<float>& g, int par, cudaStream_t st);
+void launch_fused_div(const Group<float>& g, int par, cudaStream_t st);
 void launch_fused_correct(const Group<float>& g, int par, cudaStream_t st);
 bool fused_supported(int N);
+// Sets the fused kernels' dynamic shared-memory limits (call before capture).
+void fused_prepare();
+
+// readDraw.py reductions (post.cu): centroid partials (centroid_blocks() x 4 doubles) and the
+// 9 slice planes of N*N doubles at z = zs.
+int centroid_blocks();
+template <class T> void launch_centroid(const InstDev<T>* d_all, int inst, int par, double* part, cudaStream_t st);
+template <class T>
+void launch_slice(const InstDev<T>* d_all, int inst, int par, int N, int zs, double* out, cudaStream_t st);
 
 }  // namespace ttsh

@@ -1,0 +1,104 @@
+// post.cu — readDraw.py's per-snapshot reductions on the device: the phi-weighted centroid
+// (calculate_centroid, readDraw.py:30-52), the z-slice through it (readDraw.py:222-233) and the
+// 2D vorticities of (vx, vy) and (px, py) on that slice (readDraw.py:236-237) with op.py's
+// 4th-order periodic first derivatives (d1xO4 / d1yO4, op.py:3-13).
+//
+// readDraw indexes the reshaped field as field[i][j][k] = (y, x, z), so its "centroid_x" is the
+// mean y, "centroid_y" the mean x and "centroid_z" the mean z; the slice field[:, :, idx3] is the
+// [y][x] plane at z = idx3. The outputs here keep that order.
+#include <cmath>
+#include <stdexcept>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace ttsh {
+
+namespace {
+
+constexpr int CB = 256, CT = 256;
+
+// Per-block FP64 partial sums of phi, phi*y, phi*x, phi*z (fixed reduction order).
+template <class T>
+__global__ void __launch_bounds__(CT) k_centroid(const InstDev<T>* __restrict__ insts, int inst, int par,
+                                                 double* __restrict__ part) {
+  const InstDev<T>& I = insts[inst];
+  const int N = I.N;
+  const long n = (long)N * N * N;
+  const T* phi = I.phi[par];
+  double s[4] = {0, 0, 0, 0};
+  for (long i = (long)blockIdx.x * CT + threadIdx.x; i < n; i += (long)CB * CT) {
+    const double f = (double)phi[i];
+    const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / ((long)N * N));
+    s[0] += f;
+    s[1] += f * y;
+    s[2] += f * x;
+    s[3] += f * z;
+  }
+  __shared__ double sh[4][CT / 32];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    for (int o = 16; o > 0; o >>= 1) s[q] += __shfl_down_sync(0xffffffffu, s[q], o);
+    if ((threadIdx.x & 31) == 0) sh[q][threadIdx.x >> 5] = s[q];
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double a = 0;
+    for (int w = 0; w < CT / 32; ++w) a += sh[threadIdx.x][w];
+    part[blockIdx.x * 4 + threadIdx.x] = a;
+  }
+}
+
+// The z = zs plane of the 7 snapshot fields, [y][x], and the two vorticities.
+template <class T>
+__global__ void k_slice(const InstDev<T>* __restrict__ insts, int inst, int par, int zs, double* __restrict__ out) {
+  const InstDev<T>& I = insts[inst];
+  const int N = I.N;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if (x >= N) return;
+  const size_t NN = (size_t)N * N, plane = (size_t)zs * NN;
+  const size_t o = (size_t)y * N + x;
+  const T* f[7] = {I.U[0], I.U[1], I.U[2], I.P[0], I.P[1], I.P[2], I.phi[par]};
+#pragma unroll
+  for (int q = 0; q < 7; ++q) out[q * NN + o] = (double)f[q][plane + o];
+  // op.py: d1xO4(u) = (u[x-2] - 8u[x-1] + 8u[x+1] - u[x+2]) / (12h) along x, d1yO4 along y
+  const double c = 1.0 / (12 * (double)I.ph.h);
+  auto at = [&](const T* g, int yy, int xx) {
+    yy = (yy % N + N) % N;
+    xx = (xx % N + N) % N;
+    return (double)g[plane + (size_t)yy * N + xx];
+  };
+  auto dx = [&](const T* g) {
+    return c * (at(g, y, x - 2) - 8 * at(g, y, x - 1) + 8 * at(g, y, x + 1) - at(g, y, x + 2));
+  };
+  auto dy = [&](const T* g) {
+    return c * (at(g, y - 2, x) - 8 * at(g, y - 1, x) + 8 * at(g, y + 1, x) - at(g, y + 2, x));
+  };
+  out[7 * NN + o] = dx(I.U[1]) - dy(I.U[0]);  // vortex = d1xO4(vy) - d1yO4(vx)  (readDraw.py:236)
+  out[8 * NN + o] = dx(I.P[1]) - dy(I.P[0]);  // Pvortex = d1xO4(py) - d1yO4(px) (readDraw.py:237)
+}
+
+}  // namespace
+
+int centroid_blocks() { return CB; }
+
+template <class T>
+void launch_centroid(const InstDev<T>* d_all, int inst, int par, double* part, cudaStream_t st) {
+  k_centroid<T><<<CB, CT, 0, st>>>(d_all, inst, par, part);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) throw std::runtime_error(std::string("centroid launch: ") + cudaGetErrorString(e));
+}
+
+template <class T>
+void launch_slice(const InstDev<T>* d_all, int inst, int par, int N, int zs, double* out, cudaStream_t st) {
+  k_slice<T><<<dim3((N + 127) / 128, N), 128, 0, st>>>(d_all, inst, par, zs, out);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) throw std::runtime_error(std::string("slice launch: ") + cudaGetErrorString(e));
+}
+
+template void launch_centroid<float>(const InstDev<float>*, int, int, double*, cudaStream_t);
+template void launch_centroid<double>(const InstDev<double>*, int, int, double*, cudaStream_t);
+template void launch_slice<float>(const InstDev<float>*, int, int, int, int, double*, cudaStream_t);
+template void launch_slice<double>(const InstDev<double>*, int, int, int, int, double*, cudaStream_t);
+
+}  // namespace ttsh

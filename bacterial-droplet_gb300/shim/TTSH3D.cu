@@ -27,9 +27,7 @@
 
 #include <cmath>
 #include <ctime>
-#include <fstream>
 #include <iostream>
-#include <random>
 #include <string>
 #include <vector>
 
@@ -52,7 +50,7 @@ struct ttsh_input {
 struct ttsh_ext {
   double zeta, R, xi;
   uint64_t seed;
-  int precision, k2_mode, quirks, reserved;
+  int precision, k2_mode, quirks, form;
 };
 struct ttsh_sim;
 
@@ -66,6 +64,7 @@ struct Api {
   void (*destroy)(ttsh_sim*);
   const char* (*last_error)(void);
   int (*struct_size)(int);
+  int (*init_reference)(const ttsh_input*, unsigned, const char*, double*, double*, double*, double*, double*);
 };
 
 static void* load_lib() {
@@ -120,7 +119,8 @@ int main() {
   if (!(sym(h, "ttsh_read_input", a.read_input) && sym(h, "ttsh_default_ext", a.default_ext) &&
         sym(h, "ttsh_create", a.create) && sym(h, "ttsh_set_state", a.set_state) && sym(h, "ttsh_step", a.step) &&
         sym(h, "ttsh_write_conf", a.write_conf) && sym(h, "ttsh_destroy", a.destroy) &&
-        sym(h, "ttsh_last_error", a.last_error) && sym(h, "ttsh_struct_size", a.struct_size)))
+        sym(h, "ttsh_last_error", a.last_error) && sym(h, "ttsh_struct_size", a.struct_size) &&
+        sym(h, "ttsh_init_reference", a.init_reference)))
     return 1;
   if (a.struct_size(0) != (int)sizeof(ttsh_input) || a.struct_size(1) != (int)sizeof(ttsh_ext)) {
     cout << "TTSH3D: libttsh.so structure layout mismatch" << endl;
@@ -151,28 +151,16 @@ int main() {
   const int N = P.Nx;
   const size_t n = (size_t)N * N * N;
   std::vector<double> phi(n, 0.0), Pf(3 * n, 0.0), u(3 * n, 0.0), us(3 * n, 0.0), Ps(3 * n, 0.0);
-  // InitConf (TTSH3D.cu:755-896): x outer, y, z inner; 14 draws per site in the reference order.
-  default_random_engine rng(getenv("TTSH_SEED") ? (unsigned)atol(getenv("TTSH_SEED")) : (unsigned)time(0));
-  uniform_real_distribution<double> randUR;
-  int t0 = (P.T0 + 0.1 * P.dte) / P.dte;
-  ifstream InputFile("data/conf_" + to_string(t0) + ".dat");
-  for (int i = 0; i < N; i++)
-    for (int j = 0; j < N; j++)
-      for (int k = 0; k < N; k++) {
-        const size_t idx = ((size_t)k * N + j) * N + i;
-        if (P.InitCond == 0) {
-          InputFile >> u[idx] >> u[n + idx];
-        } else if (P.InitCond == 1) {
-          double* tgt[12] = {&u[idx], &u[n + idx], &u[2 * n + idx], &us[idx], &us[n + idx], &us[2 * n + idx],
-                             &Pf[idx], &Pf[n + idx], &Pf[2 * n + idx], &Ps[idx], &Ps[n + idx], &Ps[2 * n + idx]};
-          for (int c = 0; c < 12; ++c) *tgt[c] = 0 + P.init0 * (randUR(rng) - 0.5);
-          double dx = (i - P.Nx / 2.), dy = (j - P.Ny / 2.), dz = (k - P.Nz / 2.);
-          double r = sqrt(dx * dx + dy * dy + dz * dz);
-          phi[idx] = (1 - tanh((r - P.Nx / 4.) * 2)) / 2;
-          (void)randUR(rng);  // p_v: overwritten by the first projection
-          (void)randUR(rng);  // p_p
-        }
-      }
+  // InitConf (TTSH3D.cu:755-896): the reference's own noise (x outer, y, z inner; 14 draws per
+  // site) from default_random_engine seeded by time(0) or $TTSH_SEED, or InitCond == 0's file.
+  const unsigned seed = getenv("TTSH_SEED") ? (unsigned)atol(getenv("TTSH_SEED")) : (unsigned)time(0);
+  const int t0 = (P.T0 + 0.1 * P.dte) / P.dte;
+  const std::string conf0 = "data/conf_" + to_string(t0) + ".dat";
+  rc = a.init_reference(&P, seed, conf0.c_str(), phi.data(), Pf.data(), u.data(), us.data(), Ps.data());
+  if (rc != 0) {
+    cout << "TTSH3D: " << a.last_error() << endl;
+    return 2;
+  }
   rc = a.set_state(sim, 0, phi.data(), Pf.data(), u.data(), us.data(), Ps.data());
   if (rc != 0) {
     cout << "TTSH3D: " << a.last_error() << endl;

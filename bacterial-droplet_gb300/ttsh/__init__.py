@@ -20,6 +20,7 @@ HEADER = os.path.join(os.path.dirname(PKG), "include", "ttsh.h")
 
 OK, E_INVALID, E_IO, E_PARSE, E_CUDA, E_NODEVICE, E_NOMEM, E_UNSTABLE, E_UNSUPPORTED = range(9)
 K2_REFERENCE, K2_DISCRETE = 0, 1
+FORM_AUTO, FORM_PLAIN, FORM_FUSED = 0, 1, 2
 QUIRK_STALE_HALO = 1
 READ_SUCCESS = -8848
 
@@ -42,7 +43,7 @@ class Input(ctypes.Structure):
 class Ext(ctypes.Structure):
     _fields_ = [("zeta", ctypes.c_double), ("R", ctypes.c_double), ("xi", ctypes.c_double),
                 ("seed", ctypes.c_uint64), ("precision", ctypes.c_int), ("k2_mode", ctypes.c_int),
-                ("quirks", ctypes.c_int), ("reserved", ctypes.c_int)]
+                ("quirks", ctypes.c_int), ("form", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -102,6 +103,13 @@ def lib():
                                       ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
             "ttsh_launches_per_step": ([_VP], ctypes.c_int),
             "ttsh_struct_size": ([ctypes.c_int], ctypes.c_int),
+            "ttsh_save_checkpoint": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),
+            "ttsh_init_reference": ([ctypes.POINTER(Input), ctypes.c_uint, ctypes.c_char_p, _D, _D, _D, _D, _D],
+                                    ctypes.c_int),
+            "ttsh_run_dirs": ([ctypes.POINTER(ctypes.c_char_p), ctypes.c_int, ctypes.POINTER(Ext), ctypes.c_uint64,
+                               ctypes.c_int], ctypes.c_int),
+            "ttsh_snapshot_slice": ([_VP, ctypes.c_int, _D, ctypes.POINTER(ctypes.c_int), _D], ctypes.c_int),
+            "ttsh_load_checkpoint": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),
             "ttsh_step_noalloc": ([ctypes.POINTER(Input), ctypes.POINTER(Ext), ctypes.c_int] + [_VP] * 7 + [_VP],
                                   ctypes.c_int),
         }
@@ -181,6 +189,22 @@ def init_droplet(N: int, R: float, xi: float, seed: int, h: float = 1.0, angular
     P = np.zeros((3, N, N, N))
     _check(lib().ttsh_init_droplet(N, h, R, xi, seed, angular_noise, _p(phi), _p(P)))
     return phi, P
+
+
+def init_reference(inp: Input, seed: int, conf0_path: str | None = None):
+    """The reference program's own initial state (InitConf, InitCond 1 noise or InitCond 0 file)."""
+    N = inp.Nx
+    phi = np.zeros((N, N, N))
+    P, u, us, ps = (np.zeros((3, N, N, N)) for _ in range(4))
+    _check(lib().ttsh_init_reference(ctypes.byref(inp), seed, conf0_path.encode() if conf0_path else None,
+                                     _p(phi), _p(P), _p(u), _p(us), _p(ps)))
+    return dict(phi=phi, P=P, u=u, us=us, ps=ps)
+
+
+def run_dirs(dirs, ext: Ext | None = None, seed: int = 0, device: int = -1):
+    """forEach.pl's sweep as one batched run over directories that each hold an input.dat."""
+    arr = (ctypes.c_char_p * len(dirs))(*[d.encode() for d in dirs])
+    _check(lib().ttsh_run_dirs(arr, len(dirs), ctypes.byref(ext) if ext is not None else None, seed, device))
 
 
 def format_conf(path: str, phi, P, u, expo_data: int = 1):
@@ -266,6 +290,26 @@ class Sim:
 
     def write_conf(self, inst: int, path: str):
         _check(lib().ttsh_write_conf(self._h, inst, path.encode()))
+
+    SLICE_NAMES = ("vx", "vy", "vz", "px", "py", "pz", "phi", "vortex", "Pvortex")
+
+    def snapshot_slice(self, inst: int = 0):
+        """readDraw.py's centroid, centroid z-slice and vorticities, computed on the GPU."""
+        N = self.sizes[inst]
+        c = (ctypes.c_double * 3)()
+        idx = (ctypes.c_int * 3)()
+        out = np.empty((9, N, N))
+        _check(lib().ttsh_snapshot_slice(self._h, inst, c, idx, _p(out)))
+        res = {n: out[i] for i, n in enumerate(self.SLICE_NAMES)}
+        res["centroid"] = tuple(c)
+        res["index"] = tuple(idx)
+        return res
+
+    def save_checkpoint(self, inst: int, path: str):
+        _check(lib().ttsh_save_checkpoint(self._h, inst, path.encode()))
+
+    def load_checkpoint(self, inst: int, path: str):
+        _check(lib().ttsh_load_checkpoint(self._h, inst, path.encode()))
 
     def time(self) -> float:
         return lib().ttsh_time(self._h)

@@ -17,7 +17,7 @@ LIBDIR = os.path.join(PKG, "lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libttsh.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cu", "plain.cu", "fft.cu", "fused.cu", "io.cpp", "noalloc.cu"]
+SOURCES = ["api.cu", "plain.cu", "fft.cu", "fftreg_f32.cu", "fftreg_f64.cu", "fused.cu", "io.cpp", "noalloc.cu", "post.cu"]
 
 
 def nvcc() -> str:

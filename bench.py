@@ -75,6 +75,8 @@ def workload(name: str):
         return out
     if name == "1x512":
         return [(512, 160.0, 3.0, 7, 0.02)]
+    if name == "1x128":
+        return [(128, 32.0, 2.0, 1, 0.02)]
     if name == "1x64":
         return [(64, 16.0, 2.0, 0, 0.01)]
     raise SystemExit("unknown workload " + name)
@@ -132,12 +134,12 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
-def make_sim(ttsh, drops, precision, k2_mode=0, quirks=1):
+def make_sim(ttsh, drops, precision, k2_mode=0, quirks=1, form=0):
     inps, exts = [], []
     for (N, R, xi, seed, zeta) in drops:
         inps.append(ttsh.default_input(Nx=N, Ny=N, Nz=N))
         exts.append(ttsh.default_ext(precision=precision, zeta=zeta, R=R, xi=xi, seed=seed, k2_mode=k2_mode,
-                                     quirks=quirks))
+                                     quirks=quirks, form=form))
     return ttsh.Sim(inps, exts, device=0)
 
 
@@ -235,6 +237,7 @@ def main():
     ap.add_argument("--precision", type=int, default=32, choices=[32, 64])
     ap.add_argument("--workload", default="2x256")
     ap.add_argument("--k2", type=int, default=0, choices=[0, 1])
+    ap.add_argument("--form", type=int, default=0, choices=[0, 1, 2], help="0 auto, 1 plain, 2 fused")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -260,7 +263,7 @@ def main():
 
     drops = workload(args.workload)
     sites = sum(d[0] ** 3 for d in drops)
-    sim = make_sim(ttsh, drops, args.precision, k2_mode=args.k2)
+    sim = make_sim(ttsh, drops, args.precision, k2_mode=args.k2, form=args.form)
     # one non-default stream shared by the library and the timing events
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)

@@ -60,8 +60,11 @@ typedef struct ttsh_ext {
   int precision;   /* 64 = FP64 fields and FFT, 32 = FP32 fields and FFT */
   int k2_mode;     /* TTSH_K2_REFERENCE or TTSH_K2_DISCRETE */
   int quirks;      /* bitmask of TTSH_QUIRK_* (default TTSH_QUIRK_STALE_HALO) */
-  int reserved;
+  int form;        /* TTSH_FORM_AUTO, TTSH_FORM_PLAIN or TTSH_FORM_FUSED (same for all droplets) */
 } ttsh_ext;
+#define TTSH_FORM_AUTO 0   /* fused kernels where supported (FP32, N a multiple of 32), else plain */
+#define TTSH_FORM_PLAIN 1  /* one thread per site, the reference's arithmetic order (FP64 or FP32) */
+#define TTSH_FORM_FUSED 2  /* fused FP32 kernels; TTSH_E_UNSUPPORTED where they do not apply */
 
 typedef struct ttsh_stats {
   double mass;       /* sum(phi) h^3, FP64 reduction */
@@ -110,6 +113,24 @@ int ttsh_set_state(ttsh_sim* s, int inst, const double* phi, const double* P, co
 int ttsh_init_droplet(int N, double h, double R, double xi, uint64_t seed, double angular_noise,
                       double* phi, double* P);
 
+/* InitConf's own initial state (TTSH3D.cu:755-896), host only: InitCond == 1 draws uniform noise
+ * init0*(U-1/2) for u, u*, P, P* (and two discarded draws for p_v, p_p) from
+ * std::default_random_engine(seed), 14 draws per site, x outer / y / z inner as the reference
+ * does, and phi = (1 - tanh((r - Nx/4)*2))/2; InitCond == 0 reads vx, vy (2 columns per site, the
+ * same loop order) from `conf0_path` (the reference's data/conf_<t0>.dat). Arrays as
+ * ttsh_set_state's; P, u, ustar, Pstar are 3*N^3. */
+int ttsh_init_reference(const ttsh_input* in, unsigned seed, const char* conf0_path, double* phi, double* P,
+                        double* u, double* ustar, double* Pstar);
+
+/* forEach.pl's sweep as one batched run: the reference runs one TTSH3D.out per parameter set
+ * (forEach.pl:33-131, run_cuda.pl:136). Each of the n directories holds an input.dat; all droplets
+ * advance together (one launch per kernel per size group), each with its own constants, dt, dte
+ * and Ts, starting from ttsh_init_reference(seed + i), and each writes its conf_<te>.dat files
+ * into its own directory at the times TTSH3D.out would (conf_0.dat first when T0 == 0). A droplet
+ * whose T has passed its Ts stops writing; the batch ends when all have. `ext` may be NULL
+ * (defaults) and applies to every droplet. */
+int ttsh_run_dirs(const char* const* dirs, int n, const ttsh_ext* ext, uint64_t seed, int device);
+
 /* EEuler x nsteps (TTSH3D.cu:347-359, run/evolve :336-343, :311-331): asynchronous. */
 int ttsh_step(ttsh_sim* s, int nsteps);
 
@@ -132,6 +153,24 @@ int ttsh_write_conf(ttsh_sim* s, int inst, const char* path);
 /* Same formatter on host arrays (no GPU): for writing conf files from any source. */
 int ttsh_format_conf(int N, int expo_data, const double* phi, const double* P, const double* u,
                      const char* path);
+
+/* readDraw.py's reductions of one snapshot, on the device (so no 3D text file is needed):
+ * centroid[3] = the phi-weighted mean (y, x, z) in FP64 (calculate_centroid, readDraw.py:30-52,
+ * which returns the int() of these), index[3] = those int() values, and slices = 9*N*N doubles,
+ * each a [y][x] plane at z = index[2]: vx, vy, vz, px, py, pz, phi, then the vorticities
+ * d1xO4(vy) - d1yO4(vx) and d1xO4(py) - d1yO4(px) (readDraw.py:222-237, op.py:3-13).
+ * The centroid sums are FP64 in a fixed (parallel) order; readDraw sums sequentially, so index
+ * can differ from readDraw's only when a mean lies within ~1e-12 of an integer. */
+int ttsh_snapshot_slice(ttsh_sim* s, int inst, double* centroid, int* index, double* slices);
+
+/* Checkpoint / resume (replaces the reference's T0 > 0 restart, TTSH3D.cu:769-797, which reads
+ * only vx, vy of InitCond == 0 from data/conf_<t0>.dat). The file holds T and phi, P, u, u*, P*
+ * (u*, P* feed the next step's stale halo) as the device stores them (FP32 or FP64), so a run
+ * resumed from it continues bit for bit. Layout: "TTSHCKP1", int32 version 1, int32 N, int32
+ * precision, int32 0, double T, int64 steps, then 13 arrays of N^3 (phi, P x3, u x3, u* x3, P* x3).
+ * The pressures are not stored: they are recomputed by the next step. */
+int ttsh_save_checkpoint(ttsh_sim* s, int inst, const char* path);
+int ttsh_load_checkpoint(ttsh_sim* s, int inst, const char* path);
 
 /* MemFree + cufftDestroy (TTSH3D.cu:280-281, :1275-1419). */
 void ttsh_destroy(ttsh_sim* s);

@@ -164,3 +164,20 @@ def test_conf_writer_byte_identical_to_reference_expoconf(tmp_path):
 def test_golden_fixture_script_is_committed():
     assert os.path.exists(os.path.join(ROOT, "tests", "golden", "make_ref_golden.py"))
     assert os.path.exists(os.path.join(ROOT, "tests", "golden", "make_input_dat.py"))
+
+
+OP_PY = "/root/reference/bacterial_droplet_12-16/op.py"
+
+
+@pytest.mark.skipif(not os.path.exists(OP_PY), reason="reference sources not present")
+def test_readdraw_restatement_matches_op_py():
+    """The numpy restatement of op.py's d1xO4/d1yO4 equals op.py itself (imported from the reference)."""
+    import importlib.util
+    import readdraw_restatement as RD
+    spec = importlib.util.spec_from_file_location("ref_op", OP_PY)
+    op = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(op)
+    rng = np.random.default_rng(0)
+    u = rng.standard_normal((12, 16))
+    np.testing.assert_allclose(RD.d1xO4(u, 0.7), op.d1xO4(u, 0.7), rtol=0, atol=1e-13)
+    np.testing.assert_allclose(RD.d1yO4(u, 0.7), op.d1yO4(u, 0.7), rtol=0, atol=1e-13)

@@ -2,7 +2,7 @@
 
 Tolerances (relative L2 per field, written here and in the asserts):
   FP64 plain form vs oracle: 1e-11 (differences are FMA contraction and summation order only)
-  FP32 forms vs oracle: per-field bounds stated in FP32_TOL below.
+  FP32 forms: tests/test_gpu_fp32.py.
 """
 import numpy as np
 import pytest
@@ -49,7 +49,7 @@ def field_errors(g, o):
     return {k: relerr(g[k], o[k]) for k in FIELDS}
 
 
-@pytest.mark.parametrize("N", [16, 24, 32])
+@pytest.mark.parametrize("N", [16, 20, 24, 32])
 @pytest.mark.parametrize("k2_mode,stale,zeta", [(0, 1, 0.0), (0, 1, 0.02), (1, 0, 0.02), (1, 1, 0.0)])
 def test_fp64_matches_oracle(oracle_mod, N, k2_mode, stale, zeta):
     st = random_state(N, seed=N + 7)
@@ -124,3 +124,17 @@ def test_reference_k2_is_not_solenoidal_fp64():
     st = random_state(32, seed=5)
     g = run_gpu(st, 3, 64, k2_mode=0, quirks=1)
     assert g["stats"]["max_div_u"] > 1e-8
+
+
+@pytest.mark.parametrize("N", [16, 32, 48])
+def test_fft_kernels_agree(oracle_mod, N, monkeypatch):
+    """The register-resident FFT passes and the shared-memory Stockham passes both match the oracle."""
+    st = random_state(N, seed=N + 11)
+    o = run_oracle(oracle_mod, st, 3, 0, 1, 0.01)
+    monkeypatch.setenv("TTSH_FFT", "stockham")
+    a = run_gpu(st, 3, 64, 0, 1, 0.01)
+    monkeypatch.delenv("TTSH_FFT")
+    b = run_gpu(st, 3, 64, 0, 1, 0.01)
+    for g in (a, b):
+        errs = field_errors(g, o)
+        assert max(errs.values()) <= FP64_TOL, errs
