@@ -88,6 +88,51 @@ struct HoodAcc {
   __device__ __forceinline__ float operator()(int dx, int dy, int dz) const { return h->v[1 + dz][1 + k + dy][1 + dx]; }
 };
 
+// Separable evaluation on a Hood (FP32 form). With s = [1, 4, 1] and delta = [-1, 0, 1]:
+//   D_x = c2h/36 * delta_x s_y s_z,  D_y = c2h/36 * s_x delta_y s_z,  D_z = c2h/36 * s_x s_y delta_z,
+//   L = cl12 * (8 corners) + cl23 * (6 faces) - cl143 * centre  (corners = c_x c_y c_z, c = [1, 0, 1]),
+// the reference's 27-point and 15-point weights (TTSH3D.cu:3280-3343) regrouped so that the
+// z-combinations of each (row, column) are shared by the R sites of the strip.
+struct SepK {
+  float d;  // c2h / 36
+  float l12, l23, l143;
+};
+template <int R, bool DX, bool DY, bool DZ, bool LAP>
+__device__ __forceinline__ void sep_eval(const Hood<R>& h, const SepK& k, float* dx, float* dy, float* dz, float* lap) {
+  float cz[R + 2][3], sz[R + 2][3], dzr[R + 2][3];
+#pragma unroll
+  for (int r = 0; r < R + 2; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      cz[r][c] = h.v[0][r][c] + h.v[2][r][c];
+      sz[r][c] = fmaf(4.f, h.v[1][r][c], cz[r][c]);
+      dzr[r][c] = h.v[2][r][c] - h.v[0][r][c];
+    }
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
+    if (DX) {
+      const float a = fmaf(4.f, sz[i + 1][2], sz[i][2] + sz[i + 2][2]);
+      const float b = fmaf(4.f, sz[i + 1][0], sz[i][0] + sz[i + 2][0]);
+      dx[i] = k.d * (a - b);
+    }
+    if (DY) {
+      const float e0 = sz[i + 2][0] - sz[i][0], e1 = sz[i + 2][1] - sz[i][1], e2 = sz[i + 2][2] - sz[i][2];
+      dy[i] = k.d * fmaf(4.f, e1, e0 + e2);
+    }
+    if (DZ) {
+      const float f0 = fmaf(4.f, dzr[i + 1][0], dzr[i][0] + dzr[i + 2][0]);
+      const float f1 = fmaf(4.f, dzr[i + 1][1], dzr[i][1] + dzr[i + 2][1]);
+      const float f2 = fmaf(4.f, dzr[i + 1][2], dzr[i][2] + dzr[i + 2][2]);
+      dz[i] = k.d * fmaf(4.f, f1, f0 + f2);
+    }
+    if (LAP) {
+      const float corners = (cz[i][0] + cz[i][2]) + (cz[i + 2][0] + cz[i + 2][2]);
+      const float faces = (cz[i + 1][1] + h.v[1][i + 1][0]) + (h.v[1][i + 1][2] + h.v[1][i][1]) + h.v[1][i + 2][1];
+      lap[i] = fmaf(k.l12, corners, fmaf(k.l23, faces, -k.l143 * h.v[1][i + 1][1]));
+    }
+  }
+}
+
 // Interleaved-complex variant (one component of a float2 plane).
 template <int R>
 struct Hood2 {
@@ -118,6 +163,7 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
   const int N = insts[0].N;
   const InstDev<float>& I = insts[blockIdx.z / nchunk];
   const Phys<float>& p = I.ph;
+  const SepK sk{p.c2h * (1.f / 36.f), p.cl12, p.cl23, p.cl143};
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const int z0 = (blockIdx.z % nchunk) * ZC;
   const int z1 = min(z0 + ZC, N);
@@ -178,26 +224,20 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
           Hood<RY> h;
           h.load(a0, a1, a2, AW, ax, ay0);
 #pragma unroll
-          for (int k = 0; k < RY; ++k) {
-            HoodAcc<RY> F{&h, k};
-            phc[k] = F(0, 0, 0);
-            lphi[k] = st_lap<float>(F, p);
-          }
+          for (int k = 0; k < RY; ++k) phc[k] = h.v[1][1 + k][1];
+          sep_eval<RY, false, false, false, true>(h, sk, nullptr, nullptr, nullptr, lphi);
         }
         float Pc[3][RY], DP[3][3][RY];  // DP[a][b] = D_a P_b
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
           Hood<RY> h;
           h.load(a0 + (1 + b) * AN, a1 + (1 + b) * AN, a2 + (1 + b) * AN, AW, ax, ay0);
+          float lp[RY];
+          sep_eval<RY, true, true, true, true>(h, sk, DP[0][b], DP[1][b], DP[2][b], lp);
 #pragma unroll
           for (int k = 0; k < RY; ++k) {
-            HoodAcc<RY> F{&h, k};
-            Pc[b][k] = F(0, 0, 0);
-            DP[0][b][k] = st_dx<float>(F, p.c2h);
-            DP[1][b][k] = st_dy<float>(F, p.c2h);
-            DP[2][b][k] = st_dz<float>(F, p.c2h);
-            const float lp = st_lap<float>(F, p);
-            bq[(QMU + b) * BN + (by0 + k) * BW + bx] = phc[k] * Pc[b][k] + p.La2 * lp;  // mu_b (:571-573)
+            Pc[b][k] = h.v[1][1 + k][1];
+            bq[(QMU + b) * BN + (by0 + k) * BW + bx] = fmaf(p.La2, lp[k], phc[k] * Pc[b][k]);  // mu_b (:571-573)
           }
         }
 #pragma unroll
@@ -245,13 +285,8 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
           Hood<RY> h;
           h.load(a0, a1, a2, AW, ax, ay0);
 #pragma unroll
-          for (int k = 0; k < RY; ++k) {
-            HoodAcc<RY> F{&h, k};
-            phc[k] = F(0, 0, 0);
-            dphi[0][k] = st_dx<float>(F, p.c2h);
-            dphi[1][k] = st_dy<float>(F, p.c2h);
-            dphi[2][k] = st_dz<float>(F, p.c2h);
-          }
+          for (int k = 0; k < RY; ++k) phc[k] = h.v[1][1 + k][1];
+          sep_eval<RY, true, true, true, false>(h, sk, dphi[0], dphi[1], dphi[2], nullptr);
         }
         float uc[3][RY], du[3][3][RY], lu[3][RY];  // du[b][a] = D_a u_b
 #pragma unroll
@@ -259,39 +294,40 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
           Hood<RY> h;
           h.load(u0 + b * BN, u1 + b * BN, u2 + b * BN, BW, bx, by0);
 #pragma unroll
-          for (int k = 0; k < RY; ++k) {
-            HoodAcc<RY> F{&h, k};
-            uc[b][k] = F(0, 0, 0);
-            du[b][0][k] = st_dx<float>(F, p.c2h);
-            du[b][1][k] = st_dy<float>(F, p.c2h);
-            du[b][2][k] = st_dz<float>(F, p.c2h);
-            lu[b][k] = st_lap<float>(F, p);
-          }
+          for (int k = 0; k < RY; ++k) uc[b][k] = h.v[1][1 + k][1];
+          sep_eval<RY, true, true, true, true>(h, sk, du[b][0], du[b][1], du[b][2], lu[b]);
         }
         float mu0c[RY], lmu0[RY];
         {
           Hood<RY> h;
           h.load(q0 + QMU0 * BN, q1 + QMU0 * BN, q2 + QMU0 * BN, BW, bx, by0);
 #pragma unroll
-          for (int k = 0; k < RY; ++k) {
-            HoodAcc<RY> F{&h, k};
-            mu0c[k] = F(0, 0, 0);
-            lmu0[k] = st_lap<float>(F, p);
-          }
+          for (int k = 0; k < RY; ++k) mu0c[k] = h.v[1][1 + k][1];
+          sep_eval<RY, false, false, false, true>(h, sk, nullptr, nullptr, nullptr, lmu0);
         }
         // velocity: d/dt u_b (:617-621) + the stress divergence; u*_b = u_b + dt d/dt u_b (:480-482)
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
           float fdiv[RY];
           {
-            Hood<RY> hx, hy, hz;
-            hx.load(q0 + (QS + 0 * 3 + b) * BN, q1 + (QS + 0 * 3 + b) * BN, q2 + (QS + 0 * 3 + b) * BN, BW, bx, by0);
-            hy.load(q0 + (QS + 1 * 3 + b) * BN, q1 + (QS + 1 * 3 + b) * BN, q2 + (QS + 1 * 3 + b) * BN, BW, bx, by0);
-            hz.load(q0 + (QS + 2 * 3 + b) * BN, q1 + (QS + 2 * 3 + b) * BN, q2 + (QS + 2 * 3 + b) * BN, BW, bx, by0);
+            float fx[RY], fy[RY], fz[RY];
+            {
+              Hood<RY> h;
+              h.load(q0 + (QS + 0 * 3 + b) * BN, q1 + (QS + 0 * 3 + b) * BN, q2 + (QS + 0 * 3 + b) * BN, BW, bx, by0);
+              sep_eval<RY, true, false, false, false>(h, sk, fx, nullptr, nullptr, nullptr);
+            }
+            {
+              Hood<RY> h;
+              h.load(q0 + (QS + 1 * 3 + b) * BN, q1 + (QS + 1 * 3 + b) * BN, q2 + (QS + 1 * 3 + b) * BN, BW, bx, by0);
+              sep_eval<RY, false, true, false, false>(h, sk, nullptr, fy, nullptr, nullptr);
+            }
+            {
+              Hood<RY> h;
+              h.load(q0 + (QS + 2 * 3 + b) * BN, q1 + (QS + 2 * 3 + b) * BN, q2 + (QS + 2 * 3 + b) * BN, BW, bx, by0);
+              sep_eval<RY, false, false, true, false>(h, sk, nullptr, nullptr, fz, nullptr);
+            }
 #pragma unroll
-            for (int k = 0; k < RY; ++k)
-              fdiv[k] = st_dx<float>(HoodAcc<RY>{&hx, k}, p.c2h) + st_dy<float>(HoodAcc<RY>{&hy, k}, p.c2h) +
-                        st_dz<float>(HoodAcc<RY>{&hz, k}, p.c2h);
+            for (int k = 0; k < RY; ++k) fdiv[k] = fx[k] + fy[k] + fz[k];
           }
 #pragma unroll
           for (int k = 0; k < RY; ++k) {
@@ -304,8 +340,12 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
         // polarisation: d/dt P_b (:623-629); P*_b = P_b + dt d/dt P_b (:486-488)
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
-          Hood<RY> h;
-          h.load(q0 + (QMU + b) * BN, q1 + (QMU + b) * BN, q2 + (QMU + b) * BN, BW, bx, by0);
+          float lmu[RY];
+          {
+            Hood<RY> h;
+            h.load(q0 + (QMU + b) * BN, q1 + (QMU + b) * BN, q2 + (QMU + b) * BN, BW, bx, by0);
+            sep_eval<RY, false, false, false, true>(h, sk, nullptr, nullptr, nullptr, lmu);
+          }
 #pragma unroll
           for (int k = 0; k < RY; ++k) {
             const int c = (cy0 + k) * TX + cx;
@@ -321,7 +361,7 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
             else cub = px * pz * px + py * pz * py + pz * pz * pz;
             const float Ab = dphi[0][k] * dphi[b][k] * px + dphi[1][k] * dphi[b][k] * py + dphi[2][k] * dphi[b][k] * pz;
             const float r = -uc[0][k] * dxp - uc[1][k] * dyp - uc[2][k] * dzp - p.alpha * phc[k] * pb -
-                            p.beta * P2 * pb + p.eta * st_lap<float>(HoodAcc<RY>{&h, k}, p) -
+                            p.beta * P2 * pb + p.eta * lmu[k] -
                             p.lambda0 * (px * dxp + py * dyp + pz * dzp) - p.A * (dPhi2 * cub + sqrtf(P2) * Ab);
             const size_t g = (size_t)zc * NN + (size_t)(y0 + cy0 + k) * N + (x0 + cx);
             I.Ps[par ^ 1][b][g] = pb + p.dt * r;
@@ -389,16 +429,27 @@ __global__ void __launch_bounds__(NTD) k_fused_div(const InstDev<float>* __restr
       const float* s2 = sm + (i % RR) * 6 * DN;
       const int cx = threadIdx.x % TX, cy0 = (threadIdx.x / TX) * RD;
       float d[2][RD];
+      const SepK sk{p.c2h * (1.f / 36.f), p.cl12, p.cl23, p.cl143};
 #pragma unroll
       for (int f = 0; f < 2; ++f) {
-        Hood<RD> hx, hy, hz;
-        hx.load(s0 + (3 * f + 0) * DN, s1 + (3 * f + 0) * DN, s2 + (3 * f + 0) * DN, W, cx + 1, cy0 + 1);
-        hy.load(s0 + (3 * f + 1) * DN, s1 + (3 * f + 1) * DN, s2 + (3 * f + 1) * DN, W, cx + 1, cy0 + 1);
-        hz.load(s0 + (3 * f + 2) * DN, s1 + (3 * f + 2) * DN, s2 + (3 * f + 2) * DN, W, cx + 1, cy0 + 1);
+        float gx[RD], gy[RD], gz[RD];
+        {
+          Hood<RD> h;
+          h.load(s0 + (3 * f + 0) * DN, s1 + (3 * f + 0) * DN, s2 + (3 * f + 0) * DN, W, cx + 1, cy0 + 1);
+          sep_eval<RD, true, false, false, false>(h, sk, gx, nullptr, nullptr, nullptr);
+        }
+        {
+          Hood<RD> h;
+          h.load(s0 + (3 * f + 1) * DN, s1 + (3 * f + 1) * DN, s2 + (3 * f + 1) * DN, W, cx + 1, cy0 + 1);
+          sep_eval<RD, false, true, false, false>(h, sk, nullptr, gy, nullptr, nullptr);
+        }
+        {
+          Hood<RD> h;
+          h.load(s0 + (3 * f + 2) * DN, s1 + (3 * f + 2) * DN, s2 + (3 * f + 2) * DN, W, cx + 1, cy0 + 1);
+          sep_eval<RD, false, false, true, false>(h, sk, nullptr, nullptr, gz, nullptr);
+        }
 #pragma unroll
-        for (int k = 0; k < RD; ++k)
-          d[f][k] = (st_dx<float>(HoodAcc<RD>{&hx, k}, p.c2h) + st_dy<float>(HoodAcc<RD>{&hy, k}, p.c2h) +
-                     st_dz<float>(HoodAcc<RD>{&hz, k}, p.c2h)) * p.inv_dt;
+        for (int k = 0; k < RD; ++k) d[f][k] = (gx[k] + gy[k] + gz[k]) * p.inv_dt;
       }
 #pragma unroll
       for (int k = 0; k < RD; ++k) {
@@ -453,21 +504,35 @@ __global__ void __launch_bounds__(NTD) k_fused_correct(const InstDev<float>* __r
       const int zc = z0 - 2 + i;
       const int cx = threadIdx.x % TX, cy0 = (threadIdx.x / TX) * RD;
       const float* dq = sq + ((i + 2) % 3) * 6 * TX * TY;  // staged by issue(i - 1)
-      Hood2<RD> h;
-      h.load(sm2 + ((i + RR - 2) % RR) * DN, sm2 + ((i + RR - 1) % RR) * DN, sm2 + (i % RR) * DN, W, cx + 1, cy0 + 1);
+      float gv[3][RD], gp[3][RD];
+      {
+        const SepK sk{p.c2h * (1.f / 36.f), p.cl12, p.cl23, p.cl143};
+        Hood2<RD> h2;
+        h2.load(sm2 + ((i + RR - 2) % RR) * DN, sm2 + ((i + RR - 1) % RR) * DN, sm2 + (i % RR) * DN, W, cx + 1,
+                cy0 + 1);
+        Hood<RD> hv, hp;
+#pragma unroll
+        for (int z = 0; z < 3; ++z)
+#pragma unroll
+          for (int r = 0; r < RD + 2; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              hv.v[z][r][c] = h2.v[z][r][c].x;
+              hp.v[z][r][c] = h2.v[z][r][c].y;
+            }
+        sep_eval<RD, true, true, true, false>(hv, sk, gv[0], gv[1], gv[2], nullptr);
+        sep_eval<RD, true, true, true, false>(hp, sk, gp[0], gp[1], gp[2], nullptr);
+      }
 #pragma unroll
       for (int k = 0; k < RD; ++k) {
-        Hood2Acc<RD, 0> Fv{&h, k};
-        Hood2Acc<RD, 1> Fp{&h, k};
         const int c = (cy0 + k) * TX + cx;
         const size_t g = (size_t)zc * NN + (size_t)(y0 + cy0 + k) * N + (x0 + cx);
         // getVNew (TTSH3D.cu:505-511)
-        I.U[0][g] = dq[0 * TX * TY + c] - p.dt * st_dx<float>(Fv, p.c2h);
-        I.U[1][g] = dq[1 * TX * TY + c] - p.dt * st_dy<float>(Fv, p.c2h);
-        I.U[2][g] = dq[2 * TX * TY + c] - p.dt * st_dz<float>(Fv, p.c2h);
-        I.P[0][g] = dq[3 * TX * TY + c] - p.dt * st_dx<float>(Fp, p.c2h);
-        I.P[1][g] = dq[4 * TX * TY + c] - p.dt * st_dy<float>(Fp, p.c2h);
-        I.P[2][g] = dq[5 * TX * TY + c] - p.dt * st_dz<float>(Fp, p.c2h);
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+          I.U[b][g] = dq[b * TX * TY + c] - p.dt * gv[b][k];
+          I.P[b][g] = dq[(3 + b) * TX * TY + c] - p.dt * gp[b][k];
+        }
       }
     }
   }

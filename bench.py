@@ -244,9 +244,8 @@ def main():
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from ttsh import replicas
+    rank, world, local = replicas.env_rank()
 
     if args.impl == "reference":
         if rank == 0:
@@ -288,11 +287,7 @@ def main():
     if dist:
         dist.barrier()
     clocks = sampler.stop()
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(ev0.elapsed_time(ev1), device="cuda")
     value = sites * world * args.steps / (ms / 1e3) / 1e6
     stats = [sim.reduce(i, check=False) for i in range(len(drops))]
 
@@ -327,11 +322,7 @@ def main():
             lib_rc = ttsh.lib().ttsh_get_state(sim.handle, i, ttsh._p(phi), ttsh._p(P), ttsh._p(u), None, None)
             ttsh._check(lib_rc)
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-        if dist:
-            t = torch.tensor([wall], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            wall = float(t.item())
+        wall = replicas.max_over_ranks(time.perf_counter() - t0, device="cuda")
         h2d = sum(7 * d[0] ** 3 * 8 for d in drops)
         d2h = args.steps * len(drops) * 4 * 8 * 256 + sum(7 * d[0] ** 3 * 8 for d in drops)
         e2e = {"value": sites * world * args.steps / wall / 1e6, "unit": UNIT,
