@@ -26,7 +26,7 @@ constexpr size_t smem_bytes(int axis) {
 // PASS: 0 forward x, 1 forward y, 2 forward z + Poisson multiplier + inverse z, 3 inverse y,
 // 4 inverse x scaled by 1/N^3.
 template <class T, int N1, int N2, int PASS>
-__global__ void __launch_bounds__(lines_per_cta<N1 * N2>() * N2) k_fftr(const InstDev<T>* __restrict__ insts) {
+__global__ void __launch_bounds__(lines_per_cta<N1 * N2>() * N2, (sizeof(T) == 4 && N1 * N2 >= 256 && PASS == 2) ? 3 : 1) k_fftr(const InstDev<T>* __restrict__ insts) {
   typedef typename CxT<T>::type C;
   constexpr int N = N1 * N2;
   constexpr int LB = lines_per_cta<N>();

@@ -32,25 +32,28 @@ namespace {
 
 constexpr int TX = 32, TY = 16;   // output tile (columns)
 constexpr int ZC = 64;            // z-planes per block (chunk)
-constexpr int RY = 2;             // strip length (sites per thread) in fused_rhs
-constexpr int NT = 256;           // threads of fused_rhs
+constexpr int RB = 2;             // strip length (sites per thread) of fused_rhs stage 1
+constexpr int NT = 512;           // threads of fused_rhs: one tile column each in stage 2
 
 // fused_rhs regions: A = tile + 2 (phi, P), B = tile + 1 (u, stage-1 products), C = tile.
 constexpr int AW = TX + 4, AH = TY + 4, AN = AW * AH;
 constexpr int BW = TX + 2, BH = TY + 2, BN = BW * BH;
 constexpr int CN = TX * TY;
-// shared memory (floats): A ring 5 planes x 4 fields; u ring 4 x 3; B ring 3 x 13; D P ring 2 x 9.
-// The A and u rings hold one plane more than the stencils read: the next plane is copied into
-// it (cp.async) while the current planes are being computed.
-constexpr int RA = 5, RU = 4;
+// Shared memory (floats): A ring RA planes x 4 fields; u ring RU x 3; B ring 3 planes x 13
+// products; "partials" ring 2 planes x 7 on the tile. The A and u rings hold one plane more than
+// the stencils read: the next plane is copied into it (cp.async) while the current ones compute.
+constexpr int RA = 4, RU = 4;
 constexpr int SA_OFF = 0;
 constexpr int SU_OFF = SA_OFF + RA * 4 * AN;
 constexpr int SB_OFF = SU_OFF + RU * 3 * BN;
-constexpr int SD_OFF = SB_OFF + 3 * 13 * BN;
-constexpr int RHS_SMEM_FLOATS = SD_OFF + 2 * 9 * CN;
+constexpr int SQ_OFF = SB_OFF + 3 * 13 * BN;
+constexpr int SZ_OFF = SQ_OFF + 2 * 7 * CN;
+// one plane of the stress z-combinations (s_z S_xb, s_z S_yb, delta_z S_zb) for stage 2
+constexpr int RHS_SMEM_FLOATS = SZ_OFF + 9 * BN;
 constexpr size_t RHS_SMEM = RHS_SMEM_FLOATS * sizeof(float);
-// stage-1 product slots in the B ring
+// stage-1 products in the B ring, and the pointwise parts of the update ("partials")
 constexpr int QS = 0, QMU = 9, QMU0 = 12, NQ = 13;
+constexpr int PU = 0, PP = 3, PPHI = 6;
 
 __device__ __forceinline__ int wrapN(int a, int N) { return a < 0 ? a + N : (a >= N ? a - N : a); }
 
@@ -162,7 +165,7 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
   extern __shared__ __align__(16) float sm[];
   const int N = insts[0].N;
   const InstDev<float>& I = insts[blockIdx.z / nchunk];
-  const Phys<float>& p = I.ph;
+  const Phys<float> p = I.ph;  // by value: read once, kept in registers
   const SepK sk{p.c2h * (1.f / 36.f), p.cl12, p.cl23, p.cl143};
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const int z0 = (blockIdx.z % nchunk) * ZC;
@@ -171,15 +174,20 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
   const float* __restrict__ gphi = I.phi[par];
   const float* __restrict__ gP[3] = {I.P[0], I.P[1], I.P[2]};
   const float* __restrict__ gU[3] = {I.U[0], I.U[1], I.U[2]};
-  float* sA = sm + SA_OFF;  // [slot 4][field 4][AN]
-  float* sU = sm + SU_OFF;  // [slot 3][comp 3][BN]
-  float* sB = sm + SB_OFF;  // [slot 3][q 13][BN]
-  float* sD = sm + SD_OFF;  // [slot 2][9][CN]
+  float* const oUs[3] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2]};
+  float* const oPs[3] = {I.Ps[par ^ 1][0], I.Ps[par ^ 1][1], I.Ps[par ^ 1][2]};
+  float* const ophi = I.phi[par ^ 1];
+  float* sA = sm + SA_OFF;  // [RA][4][AN]: phi, Px, Py, Pz
+  float* sU = sm + SU_OFF;  // [RU][3][BN]
+  float* sB = sm + SB_OFF;  // [3][NQ][BN]
+  float* sQ = sm + SQ_OFF;  // [2][7][CN]
+  float* sZ = sm + SZ_OFF;  // [9][BN]: z-combined stress of plane c
   const int tid = threadIdx.x;
   const int niter = (z1 - z0) + 4;
 
-  // Stage 0 of iteration i: A plane a = z0 - 2 + i (phi, P over tile+2) into A slot i % RA and,
-  // from i = 2 on, u plane a - 1 (tile+1) into u slot i % RU. Issued one iteration ahead.
+  // issue(i): A plane a = z0 - 2 + i (phi, P over tile+2) into A slot i % RA, and u plane a - 1
+  // (tile+1) into u slot i % RU. Iteration i computes stage 1 at plane b = a - 1 and stage 2 at
+  // plane c = a - 2; issue(i + 1) runs during iteration i.
   auto issue = [&](int i) {
     const int za = ((z0 - 2 + i) % N + N) % N;
     float* dst = sA + (i % RA) * 4 * AN;
@@ -191,16 +199,14 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
       cp_async4(dst + 2 * AN + t, gP[1] + g);
       cp_async4(dst + 3 * AN + t, gP[2] + g);
     }
-    if (i >= 2) {
-      const int zu = ((z0 - 3 + i) % N + N) % N;
-      float* du = sU + (i % RU) * 3 * BN;
-      for (int t = tid; t < BN; t += NT) {
-        const int by = t / BW, bx = t - by * BW;
-        const size_t g = (size_t)zu * NN + (size_t)wrapN(y0 - 1 + by, N) * N + wrapN(x0 - 1 + bx, N);
-        cp_async4(du + t, gU[0] + g);
-        cp_async4(du + BN + t, gU[1] + g);
-        cp_async4(du + 2 * BN + t, gU[2] + g);
-      }
+    const int zu = ((z0 - 3 + i) % N + N) % N;
+    float* du = sU + (i % RU) * 3 * BN;
+    for (int t = tid; t < BN; t += NT) {
+      const int by = t / BW, bx = t - by * BW;
+      const size_t g = (size_t)zu * NN + (size_t)wrapN(y0 - 1 + by, N) * N + wrapN(x0 - 1 + bx, N);
+      cp_async4(du + t, gU[0] + g);
+      cp_async4(du + BN + t, gU[1] + g);
+      cp_async4(du + 2 * BN + t, gU[2] + g);
     }
     cp_async_commit();
   };
@@ -209,42 +215,52 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
     cp_async_wait_all();
     __syncthreads();
     if (i + 1 < niter) issue(i + 1);
-    // ---- stage 1 at plane b = z0 - 3 + i over B (tile+1): mu_0, mu_b, S_ab (+ D P on the tile)
+    // ---- stage 1 at plane b = z0 - 3 + i over B (tile+1): the products mu_0, mu_b, S_ab that
+    //      stage 2 differentiates, and on the tile the pointwise parts of the update
     if (i >= 2) {
       const float* a0 = sA + ((i + RA - 2) % RA) * 4 * AN;  // plane b-1
       const float* a1 = sA + ((i + RA - 1) % RA) * 4 * AN;  // plane b
       const float* a2 = sA + (i % RA) * 4 * AN;             // plane b+1
+      const float* ub = sU + (i % RU) * 3 * BN;             // u at plane b
       float* bq = sB + (i % 3) * NQ * BN;
-      float* dq = sD + (i & 1) * 9 * CN;
-      for (int s = tid; s < BW * (BH / RY); s += NT) {
-        const int bx = s % BW, by0 = (s / BW) * RY;
-        const int ax = bx + 1, ay0 = by0 + 1;  // in A coordinates
-        float phc[RY], lphi[RY];
+      float* pq = sQ + (i & 1) * 7 * CN;
+      // strips of the B region: warps take 32 consecutive columns of one strip row (unit-stride
+      // shared-memory access); the last BW - 32 columns of every row come after them
+      constexpr int NSR = BH / RB, NMAIN = 32 * NSR, NEXTRA = (BW - 32) * NSR;
+      for (int s = tid; s < NMAIN + NEXTRA; s += NT) {
+        int bx, by0;
+        if (s < NMAIN) { bx = s & 31; by0 = (s >> 5) * RB; }
+        else { const int e = s - NMAIN; bx = 32 + e % (BW - 32); by0 = (e / (BW - 32)) * RB; }
+        const int ax = bx + 1, ay0 = by0 + 1;  // A coordinates
+        float phc[RB], lphi[RB], dphi[3][RB];
         {
-          Hood<RY> h;
+          Hood<RB> h;
           h.load(a0, a1, a2, AW, ax, ay0);
 #pragma unroll
-          for (int k = 0; k < RY; ++k) phc[k] = h.v[1][1 + k][1];
-          sep_eval<RY, false, false, false, true>(h, sk, nullptr, nullptr, nullptr, lphi);
+          for (int k = 0; k < RB; ++k) phc[k] = h.v[1][1 + k][1];
+          sep_eval<RB, true, true, true, true>(h, sk, dphi[0], dphi[1], dphi[2], lphi);
         }
-        float Pc[3][RY], DP[3][3][RY];  // DP[a][b] = D_a P_b
+        float Pc[3][RB], DP[3][3][RB];  // DP[a][b] = D_a P_b
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
-          Hood<RY> h;
+          Hood<RB> h;
           h.load(a0 + (1 + b) * AN, a1 + (1 + b) * AN, a2 + (1 + b) * AN, AW, ax, ay0);
-          float lp[RY];
-          sep_eval<RY, true, true, true, true>(h, sk, DP[0][b], DP[1][b], DP[2][b], lp);
+          float lp[RB];
+          sep_eval<RB, true, true, true, true>(h, sk, DP[0][b], DP[1][b], DP[2][b], lp);
 #pragma unroll
-          for (int k = 0; k < RY; ++k) {
+          for (int k = 0; k < RB; ++k) {
             Pc[b][k] = h.v[1][1 + k][1];
             bq[(QMU + b) * BN + (by0 + k) * BW + bx] = fmaf(p.La2, lp[k], phc[k] * Pc[b][k]);  // mu_b (:571-573)
           }
         }
 #pragma unroll
-        for (int k = 0; k < RY; ++k) {
+        for (int k = 0; k < RB; ++k) {
           const float ph = phc[k];
           const int o = (by0 + k) * BW + bx;
-          bq[QMU0 * BN + o] = p.aPhi2 * (ph - 3 * ph * ph + 2 * ph * ph * ph) - p.kPhi * lphi[k];  // mu_0 (:567)
+          const float mu0 = p.aPhi2 * (ph - 3 * ph * ph + 2 * ph * ph * ph) - p.kPhi * lphi[k];  // mu_0 (:567)
+          bq[QMU0 * BN + o] = mu0;
+          const float* bq1 = sB + ((i + 2) % 3) * NQ * BN;  // plane b-1 (this thread's own column)
+          const float* bq2 = sB + ((i + 1) % 3) * NQ * BN;  // plane b-2
 #pragma unroll
           for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -252,153 +268,126 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
               float sv = p.cA * (ph * DP[a][b][k]);  // cA * sigma_ab (:587-595)
               if (p.zeta != 0.f) sv -= p.zeta * (ph * Pc[a][k] * Pc[b][k]);
               bq[(QS + a * 3 + b) * BN + o] = sv;
+              // z-combination at plane b-1 of the stress component the divergence needs along a:
+              // s_z for a = x, y and delta_z for a = z (planes b-2, b-1, b of this column)
+              const float s2 = bq2[(QS + a * 3 + b) * BN + o], s1 = bq1[(QS + a * 3 + b) * BN + o];
+              sZ[(a * 3 + b) * BN + o] = a < 2 ? fmaf(4.f, s1, s2 + sv) : sv - s2;
             }
           const int cx = bx - 1, cy = by0 + k - 1;
           if (cx >= 0 && cx < TX && cy >= 0 && cy < TY) {
+            // pointwise parts of getDtF (:617-631) at this site of plane b
+            const int c = cy * TX + cx;
+            const float vx = ub[o], vy = ub[BN + o], vz = ub[2 * BN + o];
+            const float px = Pc[0][k], py = Pc[1][k], pz = Pc[2][k];
+            const float P2 = px * px + py * py + pz * pz;
+            const float dPhi2 = dphi[0][k] * dphi[0][k] + dphi[1][k] * dphi[1][k] + dphi[2][k] * dphi[2][k];
 #pragma unroll
-            for (int a = 0; a < 3; ++a)
-#pragma unroll
-              for (int b = 0; b < 3; ++b) dq[(a * 3 + b) * CN + cy * TX + cx] = DP[a][b][k];
+            for (int b = 0; b < 3; ++b) {
+              pq[(PU + b) * CN + c] = mu0 * dphi[b][k];  // mu_0 D_b phi
+              const float pb = Pc[b][k];
+              float cub;
+              if (b == 0) cub = px * px * px + px * py * py + px * pz * pz;
+              else if (b == 1) cub = px * py * px + py * py * py + py * pz * pz;
+              else cub = px * pz * px + py * pz * py + pz * pz * pz;
+              const float Ab = dphi[0][k] * dphi[b][k] * px + dphi[1][k] * dphi[b][k] * py + dphi[2][k] * dphi[b][k] * pz;
+              pq[(PP + b) * CN + c] = -vx * DP[0][b][k] - vy * DP[1][b][k] - vz * DP[2][b][k] - p.alpha * ph * pb -
+                                      p.beta * P2 * pb - p.lambda0 * (px * DP[0][b][k] + py * DP[1][b][k] + pz * DP[2][b][k]) -
+                                      p.A * (dPhi2 * cub + sqrtf(P2) * Ab);
+            }
+            pq[PPHI * CN + c] = -vx * dphi[0][k] - vy * dphi[1][k] - vz * dphi[2][k];
           }
         }
       }
     }
     __syncthreads();
-    // ---- stage 2 at plane c = z0 - 4 + i over the tile: d/dt u, P, phi -> u*, P*, phi'
+    // ---- stage 2 at plane c = z0 - 4 + i on the tile: u*, P*, phi'
     if (i >= 4) {
-      const int zc = z0 - 4 + i;  // in [z0, z1)
-      const float* a0 = sA + ((i + RA - 3) % RA) * 4 * AN;  // plane c-1
-      const float* a1 = sA + ((i + RA - 2) % RA) * 4 * AN;  // plane c
-      const float* a2 = sA + ((i + RA - 1) % RA) * 4 * AN;  // plane c+1
-      const float* u0 = sU + ((i + RU - 2) % RU) * 3 * BN;
-      const float* u1 = sU + ((i + RU - 1) % RU) * 3 * BN;
-      const float* u2 = sU + (i % RU) * 3 * BN;
+      const int zc = z0 - 4 + i;
+      const float* u0 = sU + ((i + RU - 2) % RU) * 3 * BN;  // plane c-1
+      const float* u1 = sU + ((i + RU - 1) % RU) * 3 * BN;  // plane c
+      const float* u2 = sU + (i % RU) * 3 * BN;             // plane c+1
       const float* q0 = sB + ((i + 1) % 3) * NQ * BN;
       const float* q1 = sB + ((i + 2) % 3) * NQ * BN;
       const float* q2 = sB + (i % 3) * NQ * BN;
-      const float* dq = sD + ((i + 1) & 1) * 9 * CN;
-      for (int s = tid; s < TX * (TY / RY); s += NT) {
-        const int cx = s % TX, cy0 = (s / TX) * RY;
-        const int bx = cx + 1, by0 = cy0 + 1, ax = cx + 2, ay0 = cy0 + 2;
-        float phc[RY], dphi[3][RY];
-        {
-          Hood<RY> h;
-          h.load(a0, a1, a2, AW, ax, ay0);
+      const float* pq = sQ + ((i + 1) & 1) * 7 * CN;        // written at iteration i - 1
+      const float* ac = sA + ((i + RA - 2) % RA) * 4 * AN;   // phi, P at plane c
+      const int cx = tid % TX, cy = tid / TX;
+      const int bx = cx + 1, by = cy + 1;
+      const int c = cy * TX + cx, oa = (cy + 2) * AW + (cx + 2);
+      const size_t g = (size_t)zc * NN + (size_t)(y0 + cy) * N + (x0 + cx);
+      float uc[3], du[3][3], lu[3];  // du[b][a] = D_a u_b
 #pragma unroll
-          for (int k = 0; k < RY; ++k) phc[k] = h.v[1][1 + k][1];
-          sep_eval<RY, true, true, true, false>(h, sk, dphi[0], dphi[1], dphi[2], nullptr);
-        }
-        float uc[3][RY], du[3][3][RY], lu[3][RY];  // du[b][a] = D_a u_b
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-          Hood<RY> h;
-          h.load(u0 + b * BN, u1 + b * BN, u2 + b * BN, BW, bx, by0);
-#pragma unroll
-          for (int k = 0; k < RY; ++k) uc[b][k] = h.v[1][1 + k][1];
-          sep_eval<RY, true, true, true, true>(h, sk, du[b][0], du[b][1], du[b][2], lu[b]);
-        }
-        float mu0c[RY], lmu0[RY];
-        {
-          Hood<RY> h;
-          h.load(q0 + QMU0 * BN, q1 + QMU0 * BN, q2 + QMU0 * BN, BW, bx, by0);
-#pragma unroll
-          for (int k = 0; k < RY; ++k) mu0c[k] = h.v[1][1 + k][1];
-          sep_eval<RY, false, false, false, true>(h, sk, nullptr, nullptr, nullptr, lmu0);
-        }
-        // velocity: d/dt u_b (:617-621) + the stress divergence; u*_b = u_b + dt d/dt u_b (:480-482)
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-          float fdiv[RY];
-          {
-            float fx[RY], fy[RY], fz[RY];
-            {
-              Hood<RY> h;
-              h.load(q0 + (QS + 0 * 3 + b) * BN, q1 + (QS + 0 * 3 + b) * BN, q2 + (QS + 0 * 3 + b) * BN, BW, bx, by0);
-              sep_eval<RY, true, false, false, false>(h, sk, fx, nullptr, nullptr, nullptr);
-            }
-            {
-              Hood<RY> h;
-              h.load(q0 + (QS + 1 * 3 + b) * BN, q1 + (QS + 1 * 3 + b) * BN, q2 + (QS + 1 * 3 + b) * BN, BW, bx, by0);
-              sep_eval<RY, false, true, false, false>(h, sk, nullptr, fy, nullptr, nullptr);
-            }
-            {
-              Hood<RY> h;
-              h.load(q0 + (QS + 2 * 3 + b) * BN, q1 + (QS + 2 * 3 + b) * BN, q2 + (QS + 2 * 3 + b) * BN, BW, bx, by0);
-              sep_eval<RY, false, false, true, false>(h, sk, nullptr, nullptr, fz, nullptr);
-            }
-#pragma unroll
-            for (int k = 0; k < RY; ++k) fdiv[k] = fx[k] + fy[k] + fz[k];
-          }
-#pragma unroll
-          for (int k = 0; k < RY; ++k) {
-            const float r = -uc[0][k] * du[b][0][k] - uc[1][k] * du[b][1][k] - uc[2][k] * du[b][2][k] +
-                            p.mu * lu[b][k] + mu0c[k] * dphi[b][k] + fdiv[k];
-            const size_t g = (size_t)zc * NN + (size_t)(y0 + cy0 + k) * N + (x0 + cx);
-            I.Us[par ^ 1][b][g] = uc[b][k] + p.dt * r;
-          }
-        }
-        // polarisation: d/dt P_b (:623-629); P*_b = P_b + dt d/dt P_b (:486-488)
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-          float lmu[RY];
-          {
-            Hood<RY> h;
-            h.load(q0 + (QMU + b) * BN, q1 + (QMU + b) * BN, q2 + (QMU + b) * BN, BW, bx, by0);
-            sep_eval<RY, false, false, false, true>(h, sk, nullptr, nullptr, nullptr, lmu);
-          }
-#pragma unroll
-          for (int k = 0; k < RY; ++k) {
-            const int c = (cy0 + k) * TX + cx;
-            const float px = a1[1 * AN + (ay0 + k) * AW + ax], py = a1[2 * AN + (ay0 + k) * AW + ax],
-                        pz = a1[3 * AN + (ay0 + k) * AW + ax];
-            const float pb = b == 0 ? px : (b == 1 ? py : pz);
-            const float dxp = dq[(0 * 3 + b) * CN + c], dyp = dq[(1 * 3 + b) * CN + c], dzp = dq[(2 * 3 + b) * CN + c];
-            const float P2 = px * px + py * py + pz * pz;
-            const float dPhi2 = dphi[0][k] * dphi[0][k] + dphi[1][k] * dphi[1][k] + dphi[2][k] * dphi[2][k];
-            float cub;
-            if (b == 0) cub = px * px * px + px * py * py + px * pz * pz;
-            else if (b == 1) cub = px * py * px + py * py * py + py * pz * pz;
-            else cub = px * pz * px + py * pz * py + pz * pz * pz;
-            const float Ab = dphi[0][k] * dphi[b][k] * px + dphi[1][k] * dphi[b][k] * py + dphi[2][k] * dphi[b][k] * pz;
-            const float r = -uc[0][k] * dxp - uc[1][k] * dyp - uc[2][k] * dzp - p.alpha * phc[k] * pb -
-                            p.beta * P2 * pb + p.eta * lmu[k] -
-                            p.lambda0 * (px * dxp + py * dyp + pz * dzp) - p.A * (dPhi2 * cub + sqrtf(P2) * Ab);
-            const size_t g = (size_t)zc * NN + (size_t)(y0 + cy0 + k) * N + (x0 + cx);
-            I.Ps[par ^ 1][b][g] = pb + p.dt * r;
-          }
-        }
-        // phi: d/dt phi (:631), phi' = phi + dt d/dt phi (:515)
-#pragma unroll
-        for (int k = 0; k < RY; ++k) {
-          const float dtphi = -uc[0][k] * dphi[0][k] - uc[1][k] * dphi[1][k] - uc[2][k] * dphi[2][k] + p.gamma * lmu0[k];
-          const size_t g = (size_t)zc * NN + (size_t)(y0 + cy0 + k) * N + (x0 + cx);
-          I.phi[par ^ 1][g] = phc[k] + p.dt * dtphi;
-        }
+      for (int b = 0; b < 3; ++b) {
+        Hood<1> h;
+        h.load(u0 + b * BN, u1 + b * BN, u2 + b * BN, BW, bx, by);
+        uc[b] = h.v[1][1][1];
+        sep_eval<1, true, true, true, true>(h, sk, &du[b][0], &du[b][1], &du[b][2], &lu[b]);
       }
+      // velocity: d/dt u_b (:617-621) + the stress divergence; u*_b = u_b + dt d/dt u_b (:480-482)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        // divergence of stress column b from the z-combined plane: delta_x s_y, s_x delta_y, s_x s_y
+        float fx, fy, fz;
+        {
+          const float* Z1 = sZ + (0 * 3 + b) * BN;
+          const float* Z2 = sZ + (1 * 3 + b) * BN;
+          const float* Z3 = sZ + (2 * 3 + b) * BN;
+          const int o = by * BW + bx;
+          auto sy = [&](const float* Z, int dx) { return fmaf(4.f, Z[o + dx], Z[o + dx - BW] + Z[o + dx + BW]); };
+          auto dy = [&](const float* Z, int dx) { return Z[o + dx + BW] - Z[o + dx - BW]; };
+          fx = sk.d * (sy(Z1, 1) - sy(Z1, -1));
+          fy = sk.d * fmaf(4.f, dy(Z2, 0), dy(Z2, -1) + dy(Z2, 1));
+          fz = sk.d * fmaf(4.f, sy(Z3, 0), sy(Z3, -1) + sy(Z3, 1));
+        }
+        const float r = -uc[0] * du[b][0] - uc[1] * du[b][1] - uc[2] * du[b][2] + p.mu * lu[b] +
+                        pq[(PU + b) * CN + c] + (fx + fy + fz);
+        oUs[b][g] = uc[b] + p.dt * r;
+      }
+      // polarisation: d/dt P_b = (pointwise part) + eta L mu_b (:623-629); P*_b (:486-488)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        float lmu;
+        {
+          Hood<1> h;
+          h.load(q0 + (QMU + b) * BN, q1 + (QMU + b) * BN, q2 + (QMU + b) * BN, BW, bx, by);
+          sep_eval<1, false, false, false, true>(h, sk, nullptr, nullptr, nullptr, &lmu);
+        }
+        oPs[b][g] = ac[(1 + b) * AN + oa] + p.dt * (pq[(PP + b) * CN + c] + p.eta * lmu);
+      }
+      // phi: d/dt phi = -u.D phi + gamma L mu_0 (:631); phi' = phi + dt d/dt phi (:515)
+      float lmu0;
+      {
+        Hood<1> h;
+        h.load(q0 + QMU0 * BN, q1 + QMU0 * BN, q2 + QMU0 * BN, BW, bx, by);
+        sep_eval<1, false, false, false, true>(h, sk, nullptr, nullptr, nullptr, &lmu0);
+      }
+      ophi[g] = ac[oa] + p.dt * (pq[PPHI * CN + c] + p.gamma * lmu0);
     }
   }
 }
 
 // ------------------------------------------------------------------------------------------
 // fused_div / fused_correct: one ring of 3 planes over tile+1, strips of RD sites.
-constexpr int RD = 4;
-constexpr int NTD = TX * TY / RD;  // 128 threads
+constexpr int RD = 2;
+constexpr int NTD = TX * TY / RD;  // 256 threads
 constexpr int DN = (TX + 2) * (TY + 2);
 constexpr int RR = 4;  // ring planes of fused_div / fused_correct (3 read + 1 in flight)
 constexpr size_t DIV_SMEM = RR * 6 * DN * sizeof(float);
 constexpr size_t COR_SMEM = RR * DN * sizeof(float2) + 3 * 6 * TX * TY * sizeof(float);
 
-__global__ void __launch_bounds__(NTD) k_fused_div(const InstDev<float>* __restrict__ insts, int par, int nchunk) {
+__global__ void __launch_bounds__(NTD, 3) k_fused_div(const InstDev<float>* __restrict__ insts, int par, int nchunk) {
   extern __shared__ __align__(16) float sm[];
   const int N = insts[0].N;
   const InstDev<float>& I = insts[blockIdx.z / nchunk];
-  const Phys<float>& p = I.ph;
+  const Phys<float> p = I.ph;  // by value: read once, kept in registers
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const int z0 = (blockIdx.z % nchunk) * ZC, z1 = min(z0 + ZC, N);
   const size_t NN = (size_t)N * N;
   const float* cur[6] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2],
                          I.Ps[par ^ 1][0], I.Ps[par ^ 1][1], I.Ps[par ^ 1][2]};
   const float* old[6] = {I.Us[par][0], I.Us[par][1], I.Us[par][2], I.Ps[par][0], I.Ps[par][1], I.Ps[par][2]};
+  float2* const oW = I.W;
+  const int stale_q2 = I.stale;
   const int W = TX + 2;
   const int niter = (z1 - z0) + 2;
   // plane z0 - 1 + i into slot i % RR, issued one iteration ahead
@@ -410,7 +399,7 @@ __global__ void __launch_bounds__(NTD) k_fused_div(const InstDev<float>* __restr
     for (int t = threadIdx.x; t < DN; t += NTD) {
       const int ry = t / W, rx = t - ry * W;
       const int gx = x0 - 1 + rx, gy = y0 - 1 + ry;
-      const bool stale = I.stale && (zw || gx < 0 || gx >= N || gy < 0 || gy >= N);
+      const bool stale = stale_q2 && (zw || gx < 0 || gx >= N || gy < 0 || gy >= N);
       const size_t g = (size_t)zz * NN + (size_t)wrapN(gy, N) * N + wrapN(gx, N);
 #pragma unroll
       for (int f = 0; f < 6; ++f) cp_async4(dst + f * DN + t, (stale ? old[f] : cur[f]) + g);
@@ -454,18 +443,18 @@ __global__ void __launch_bounds__(NTD) k_fused_div(const InstDev<float>* __restr
 #pragma unroll
       for (int k = 0; k < RD; ++k) {
         const size_t g = (size_t)zc * NN + (size_t)(y0 + cy0 + k) * N + (x0 + cx);
-        I.W[g] = make_float2(d[0][k], d[1][k]);
+        oW[g] = make_float2(d[0][k], d[1][k]);
       }
     }
   }
 }
 
-__global__ void __launch_bounds__(NTD) k_fused_correct(const InstDev<float>* __restrict__ insts, int par, int nchunk) {
+__global__ void __launch_bounds__(NTD, 3) k_fused_correct(const InstDev<float>* __restrict__ insts, int par, int nchunk) {
   extern __shared__ __align__(16) float2 sm2[];
   float* sq = reinterpret_cast<float*>(sm2 + RR * DN);  // [3][6][TX*TY]: u*, P* of the compute planes
   const int N = insts[0].N;
   const InstDev<float>& I = insts[blockIdx.z / nchunk];
-  const Phys<float>& p = I.ph;
+  const Phys<float> p = I.ph;  // by value: read once, kept in registers
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const int z0 = (blockIdx.z % nchunk) * ZC, z1 = min(z0 + ZC, N);
   const size_t NN = (size_t)N * N;
@@ -473,6 +462,9 @@ __global__ void __launch_bounds__(NTD) k_fused_correct(const InstDev<float>* __r
   const int niter = (z1 - z0) + 2;
   const float* qs[6] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2],
                         I.Ps[par ^ 1][0], I.Ps[par ^ 1][1], I.Ps[par ^ 1][2]};
+  float* const oU[3] = {I.U[0], I.U[1], I.U[2]};
+  float* const oP[3] = {I.P[0], I.P[1], I.P[2]};
+  const float2* __restrict__ gW = I.W;
   // issue(i): W plane z0 - 1 + i into ring slot i % RR, and u*, P* of plane z0 - 1 + i (computed at
   // iteration i + 1) into slot i % 3. issue(i + 1) runs during iteration i, while iteration i reads
   // the u*, P* slot (i - 1) % 3 and issue(i) has filled slot i % 3.
@@ -481,7 +473,7 @@ __global__ void __launch_bounds__(NTD) k_fused_correct(const InstDev<float>* __r
     float2* dst = sm2 + (i % RR) * DN;
     for (int t = threadIdx.x; t < DN; t += NTD) {
       const int ry = t / W, rx = t - ry * W;
-      cp_async8(dst + t, I.W + (size_t)zz * NN + (size_t)wrapN(y0 - 1 + ry, N) * N + wrapN(x0 - 1 + rx, N));
+      cp_async8(dst + t, gW + (size_t)zz * NN + (size_t)wrapN(y0 - 1 + ry, N) * N + wrapN(x0 - 1 + rx, N));
     }
     const int zq = z0 - 1 + i;
     if (zq >= z0 && zq < z1) {
@@ -530,8 +522,8 @@ __global__ void __launch_bounds__(NTD) k_fused_correct(const InstDev<float>* __r
         // getVNew (TTSH3D.cu:505-511)
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
-          I.U[b][g] = dq[b * TX * TY + c] - p.dt * gv[b][k];
-          I.P[b][g] = dq[(3 + b) * TX * TY + c] - p.dt * gp[b][k];
+          oU[b][g] = dq[b * TX * TY + c] - p.dt * gv[b][k];
+          oP[b][g] = dq[(3 + b) * TX * TY + c] - p.dt * gp[b][k];
         }
       }
     }
