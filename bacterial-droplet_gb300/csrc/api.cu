@@ -278,9 +278,8 @@ void build_engine(ttsh_sim* s, Engine<T>& E) {
     const int N = ih.N;
     const size_t nn = (size_t)N * N * N;
     const size_t fb = align256(nn * sizeof(T));
-    const int nfields = 2 + 3 + 3 + 6 + 6 + (s->fused ? 0 : 13);
-    const size_t red_bytes = align256(4 * sizeof(double) * (size_t)stats_partials_per_instance(N));
-    const size_t bytes = nfields * fb + align256(nn * sizeof(C)) + red_bytes;
+    const int nfields = 2 + 3 + 3 + 6 + 6 + (s->fused ? 1 : 13);
+    const size_t bytes = nfields * fb + align256(nn * sizeof(C));
     char* d = nullptr;
     cudaError_t e = cudaMalloc(&d, bytes);
     if (e != cudaSuccess) throw std::bad_alloc();
@@ -304,17 +303,23 @@ void build_engine(ttsh_sim* s, Engine<T>& E) {
       for (int b = 0; b < 3; ++b) I.Us[q][b] = take();
     for (int q = 0; q < 2; ++q)
       for (int b = 0; b < 3; ++b) I.Ps[q][b] = take();
+    if (s->fused) I.phic = take();
     if (!s->fused) {
       I.mu0 = take();
       for (int b = 0; b < 3; ++b) I.mu[b] = take();
       for (int b = 0; b < 9; ++b) I.sig[b] = take();
     }
     I.W = reinterpret_cast<C*>(d + off);
-    off += align256(nn * sizeof(C));
-    I.red = reinterpret_cast<double*>(d + off);
   }
   for (size_t g = 0; g < E.members.size(); ++g) {
+    // FP64 diagnostics partials of all droplets of the group, contiguous (one copy back)
+    const size_t per = 4 * (size_t)stats_partials_per_instance(0);
+    double* red = nullptr;
+    CK(cudaMalloc(&red, per * E.members[g].size() * sizeof(double)));
+    s->tables.push_back(red);
+    for (size_t k = 0; k < E.members[g].size(); ++k) E.h[E.members[g][k]].red = red + k * per;
     Group<T> G{};
+    G.red = red;
     const char* fk = std::getenv("TTSH_FFT");  // "stockham": shared-memory Stockham passes only
     G.fft_kind = (fk && std::string(fk) == "stockham") ? 1 : 0;
     G.n = (int)E.members[g].size();
@@ -412,8 +417,11 @@ static void d2h(double* dst, const T* src, size_t n, cudaStream_t st, size_t str
     CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
   } else {
-    std::vector<T> tmp(n * stride);
-    CK(cudaMemcpyAsync(tmp.data(), src, n * stride * sizeof(T), cudaMemcpyDeviceToHost, st));
+    // the span from the first to the last strided element only: the odd component of an
+    // interleaved array ends one element before the array does
+    const size_t span = n == 0 ? 0 : (n - 1) * stride + 1;
+    std::vector<T> tmp(span);
+    if (span) CK(cudaMemcpyAsync(tmp.data(), src, span * sizeof(T), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     for (size_t i = 0; i < n; ++i) dst[i] = (double)tmp[i * stride];
   }
@@ -428,6 +436,7 @@ static std::vector<void*> state_arrays(ttsh_sim* s, E& eng, int inst) {
   for (int b = 0; b < 3; ++b) a.push_back(I.U[b]);
   for (int b = 0; b < 3; ++b) a.push_back(I.Us[s->par][b]);
   for (int b = 0; b < 3; ++b) a.push_back(I.Ps[s->par][b]);
+  if (I.phic) a.push_back(I.phic);  // fused form: the phi-update compensation (14th array)
   return a;
 }
 
@@ -542,6 +551,7 @@ int ttsh_set_state(ttsh_sim* s, int inst, const double* phi, const double* P, co
       auto& I = E.h[inst];
       typedef typename std::decay<decltype(*I.phi[0])>::type TT;
       h2d<TT>(I.phi[s->par], phi, n, s->stream);
+      if (I.phic) CK(cudaMemsetAsync(I.phic, 0, n * sizeof(TT), s->stream));
       for (int b = 0; b < 3; ++b) {
         h2d<TT>(I.P[b], P + b * n, n, s->stream);
         h2d<TT>(I.U[b], u + b * n, n, s->stream);
@@ -655,6 +665,47 @@ int ttsh_reduce(ttsh_sim* s, int inst, ttsh_stats* out) {
     out->nonfinite = bad > 0 ? 1 : 0;
     out->reserved = 0;
     return bad > 0 ? set_error(TTSH_E_UNSTABLE, "non-finite values in the state") : TTSH_OK;
+  });
+}
+
+int ttsh_reduce_all(ttsh_sim* s, int what, ttsh_stats* out) {
+  if (!s || !out) return set_error(TTSH_E_INVALID, "null argument");
+  if (what != TTSH_STATS_ALL && what != TTSH_STATS_MASS) return set_error(TTSH_E_INVALID, "bad stats selector");
+  return guarded([&]() -> int {
+    CK(cudaSetDevice(s->device));
+    int bad_any = 0;
+    s->with_engine([&](auto& E) {
+      const size_t per = 4 * (size_t)stats_partials_per_instance(0);
+      for (size_t g = 0; g < E.groups.size(); ++g) {
+        const auto& G = E.groups[g];
+        launch_stats(G, s->par, s->stream, what == TTSH_STATS_ALL);
+        std::vector<double> part(per * G.n);
+        CK(cudaMemcpyAsync(part.data(), G.red, part.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        for (int k = 0; k < G.n; ++k) {
+          const int inst = E.members[g][k];
+          double sum = 0, md = 0, mu = 0, bad = 0;
+          for (size_t b = 0; b < per / 4; ++b) {
+            const double* q = &part[k * per + 4 * b];
+            sum += q[0];
+            md = std::max(md, q[1]);
+            mu = std::max(mu, q[2]);
+            bad += q[3];
+          }
+          const double h = s->inst[inst].in.h;
+          ttsh_stats& o = out[inst];
+          o.mass = sum * h * h * h;
+          o.max_div_u = what == TTSH_STATS_ALL ? md : -1.0;
+          o.max_abs_u = what == TTSH_STATS_ALL ? mu : -1.0;
+          o.T = s->inst[inst].T;
+          o.steps = s->steps;
+          o.nonfinite = bad > 0 ? 1 : 0;
+          o.reserved = 0;
+          if (bad > 0) bad_any = 1;
+        }
+      }
+    });
+    return bad_any ? set_error(TTSH_E_UNSTABLE, "non-finite values in the state") : TTSH_OK;
   });
 }
 
@@ -803,14 +854,14 @@ int ttsh_save_checkpoint(ttsh_sim* s, int inst, const char* path) {
     const size_t n = (size_t)N * N * N, es = s->precision == 32 ? 4 : 8;
     FILE* fp = std::fopen(path, "wb");
     if (!fp) return set_error(TTSH_E_IO, std::string("cannot open ") + path);
-    int32_t hdr[4] = {1, N, s->precision, 0};
+    std::vector<void*> arr;
+    s->with_engine([&](auto& E) { arr = state_arrays(s, E, inst); });
+    int32_t hdr[4] = {1, N, s->precision, (int32_t)arr.size() - 13};
     double T = s->inst[inst].T;
     int64_t steps = s->steps;
     bool ok = std::fwrite(kCkpMagic, 1, 8, fp) == 8 && std::fwrite(hdr, 4, 4, fp) == 4 &&
               std::fwrite(&T, 8, 1, fp) == 1 && std::fwrite(&steps, 8, 1, fp) == 1;
     std::vector<char> buf(n * es);
-    std::vector<void*> arr;
-    s->with_engine([&](auto& E) { arr = state_arrays(s, E, inst); });
     for (void* d : arr) {
       if (!ok) break;
       CK(cudaMemcpy(buf.data(), d, n * es, cudaMemcpyDeviceToHost));
@@ -842,13 +893,13 @@ int ttsh_load_checkpoint(ttsh_sim* s, int inst, const char* path) {
       std::fclose(fp);
       return set_error(TTSH_E_PARSE, std::string("not a ttsh checkpoint: ") + path);
     }
-    if (hdr[1] != N || hdr[2] != s->precision) {
-      std::fclose(fp);
-      return set_error(TTSH_E_INVALID, "checkpoint size or precision differs from the instance");
-    }
-    std::vector<char> buf(n * es);
     std::vector<void*> arr;
     s->with_engine([&](auto& E) { arr = state_arrays(s, E, inst); });
+    if (hdr[1] != N || hdr[2] != s->precision || hdr[3] != (int32_t)arr.size() - 13) {
+      std::fclose(fp);
+      return set_error(TTSH_E_INVALID, "checkpoint size, precision or form differs from the instance");
+    }
+    std::vector<char> buf(n * es);
     for (void* d : arr) {
       if (std::fread(buf.data(), 1, n * es, fp) != n * es) {
         std::fclose(fp);

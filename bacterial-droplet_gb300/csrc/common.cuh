@@ -38,6 +38,7 @@ struct InstDev {
   T* Us[2][3];
   T* Ps[2][3];
   C* W;               // N^3 complex: (div u* + i div P*)/dt -> (p_v + i p_p)
+  T* phic;            // fused form: compensation of the phi update (the low part lost to rounding)
   T* mu0;             // plain-form intermediates
   T* mu[3];
   T* sig[9];          // sig[a*3+b] = phi * D_a P_b

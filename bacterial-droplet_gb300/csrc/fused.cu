@@ -177,6 +177,7 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
   float* const oUs[3] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2]};
   float* const oPs[3] = {I.Ps[par ^ 1][0], I.Ps[par ^ 1][1], I.Ps[par ^ 1][2]};
   float* const ophi = I.phi[par ^ 1];
+  float* const phic = I.phic;
   float* sA = sm + SA_OFF;  // [RA][4][AN]: phi, Px, Py, Pz
   float* sU = sm + SU_OFF;  // [RU][3][BN]
   float* sB = sm + SB_OFF;  // [3][NQ][BN]
@@ -210,11 +211,17 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
     }
     cp_async_commit();
   };
+  // stage-2 site of this thread (one site per thread of the tile)
+  const int qx = tid % TX, qy = tid / TX;
+  const size_t gc = (size_t)(y0 + qy) * N + (x0 + qx);
   issue(0);
   for (int i = 0; i < niter; ++i) {
     cp_async_wait_all();
     __syncthreads();
     if (i + 1 < niter) issue(i + 1);
+    // the phi compensation of this iteration's stage-2 site, loaded before stage 1 so that the
+    // stage-1 work covers the load
+    const float cprev = i >= 4 ? phic[(size_t)(z0 - 4 + i) * NN + gc] : 0.f;
     // ---- stage 1 at plane b = z0 - 3 + i over B (tile+1): the products mu_0, mu_b, S_ab that
     //      stage 2 differentiates, and on the tile the pointwise parts of the update
     if (i >= 2) {
@@ -311,10 +318,9 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
       const float* q2 = sB + (i % 3) * NQ * BN;
       const float* pq = sQ + ((i + 1) & 1) * 7 * CN;        // written at iteration i - 1
       const float* ac = sA + ((i + RA - 2) % RA) * 4 * AN;   // phi, P at plane c
-      const int cx = tid % TX, cy = tid / TX;
-      const int bx = cx + 1, by = cy + 1;
-      const int c = cy * TX + cx, oa = (cy + 2) * AW + (cx + 2);
-      const size_t g = (size_t)zc * NN + (size_t)(y0 + cy) * N + (x0 + cx);
+      const int bx = qx + 1, by = qy + 1;
+      const int c = qy * TX + qx, oa = (qy + 2) * AW + (qx + 2);
+      const size_t g = (size_t)zc * NN + gc;
       float uc[3], du[3][3], lu[3];  // du[b][a] = D_a u_b
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
@@ -361,7 +367,13 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
         h.load(q0 + QMU0 * BN, q1 + QMU0 * BN, q2 + QMU0 * BN, BW, bx, by);
         sep_eval<1, false, false, false, true>(h, sk, nullptr, nullptr, nullptr, &lmu0);
       }
-      ophi[g] = ac[oa] + p.dt * (pq[PPHI * CN + c] + p.gamma * lmu0);
+      // compensated update: the part of dt*dphi/dt that rounding drops from phi is carried to the
+      // next step (otherwise increments below half an ulp of phi are lost, a systematic mass drift)
+      const float ph = ac[oa];
+      const float inc = fmaf(p.dt, pq[PPHI * CN + c] + p.gamma * lmu0, cprev);
+      const float nv = ph + inc;
+      phic[g] = inc - (nv - ph);
+      ophi[g] = nv;
     }
   }
 }

@@ -13,6 +13,7 @@ struct Group {
   int n;               // instances in the group
   int N;
   int fft_kind = 0;    // 0: register-resident FFT kernels where the size has them; 1: Stockham only
+  double* red = nullptr;  // FP64 diagnostics partials of the whole group (n x 4 x blocks), contiguous
 };
 
 // Plain form (one thread per site, reference arithmetic order), plain.cu.
@@ -21,7 +22,7 @@ template <class T> void launch_stage2(const Group<T>& g, int par, cudaStream_t s
 template <class T> void launch_div(const Group<T>& g, int par, cudaStream_t st);
 template <class T> void launch_correct(const Group<T>& g, int par, cudaStream_t st);
 // FP64 diagnostics: per-instance partials into d_inst[i].red (nblocks_out per instance).
-template <class T> int launch_stats(const Group<T>& g, int par, cudaStream_t st);
+template <class T> int launch_stats(const Group<T>& g, int par, cudaStream_t st, bool full = true);
 int stats_partials_per_instance(int N);
 
 // Poisson solve by FFT (fft.cu): W <- (inverse FFT of -FFT(W)/k^2) / N^3.

@@ -183,7 +183,7 @@ constexpr int STATS_BLOCKS = 256, STATS_THREADS = 256;
 
 // FP64 diagnostics of the current state (phi[par], u, P): per block, sum(phi),
 // max |D.u|, max |u|, and a non-finite count. Fixed reduction order.
-template <class T>
+template <class T, bool FULL>
 __global__ void __launch_bounds__(STATS_THREADS) k_stats(const InstDev<T>* __restrict__ insts, int par) {
   const InstDev<T>& I = insts[blockIdx.y];
   const int N = I.N;
@@ -194,9 +194,11 @@ __global__ void __launch_bounds__(STATS_THREADS) k_stats(const InstDev<T>* __res
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / ((long)N * N));
     Site s;
-    s.init(x, y, z, N);
+    if (FULL) s.init(x, y, z, N);
     const double ph = (double)phi[i];
     sum += ph;
+    if (!isfinite(ph)) bad += 1;
+    if (!FULL) continue;
     const double d = (double)st_dx<T>(s.acc<T>(I.U[0]), p.c2h) + (double)st_dy<T>(s.acc<T>(I.U[1]), p.c2h) +
                      (double)st_dz<T>(s.acc<T>(I.U[2]), p.c2h);
     mdiv = fmax(mdiv, fabs(d));
@@ -205,7 +207,6 @@ __global__ void __launch_bounds__(STATS_THREADS) k_stats(const InstDev<T>* __res
       mu = fmax(mu, fabs(u));
       if (!isfinite(u) || !isfinite(q)) bad += 1;
     }
-    if (!isfinite(ph)) bad += 1;
   }
   __shared__ double sh[4][STATS_THREADS / 32];
   for (int o = 16; o > 0; o >>= 1) {
@@ -252,8 +253,9 @@ void launch_correct(const Group<T>& g, int par, cudaStream_t st) {
   check_launch("correct");
 }
 template <class T>
-int launch_stats(const Group<T>& g, int par, cudaStream_t st) {
-  k_stats<T><<<dim3(STATS_BLOCKS, g.n), STATS_THREADS, 0, st>>>(g.d_inst, par);
+int launch_stats(const Group<T>& g, int par, cudaStream_t st, bool full) {
+  if (full) k_stats<T, true><<<dim3(STATS_BLOCKS, g.n), STATS_THREADS, 0, st>>>(g.d_inst, par);
+  else k_stats<T, false><<<dim3(STATS_BLOCKS, g.n), STATS_THREADS, 0, st>>>(g.d_inst, par);
   check_launch("stats");
   return STATS_BLOCKS;
 }
@@ -263,7 +265,7 @@ int launch_stats(const Group<T>& g, int par, cudaStream_t st) {
   template void launch_stage2<T>(const Group<T>&, int, cudaStream_t);   \
   template void launch_div<T>(const Group<T>&, int, cudaStream_t);      \
   template void launch_correct<T>(const Group<T>&, int, cudaStream_t);  \
-  template int launch_stats<T>(const Group<T>&, int, cudaStream_t);
+  template int launch_stats<T>(const Group<T>&, int, cudaStream_t, bool);
 INST(float)
 INST(double)
 #undef INST

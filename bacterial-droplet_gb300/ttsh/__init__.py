@@ -92,6 +92,7 @@ def lib():
             "ttsh_get_provisional": ([_VP, ctypes.c_int, _D, _D], ctypes.c_int),
             "ttsh_reduce": ([_VP, ctypes.c_int, ctypes.POINTER(Stats)], ctypes.c_int),
             "ttsh_write_conf": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),
+            "ttsh_reduce_all": ([_VP, ctypes.c_int, ctypes.POINTER(Stats)], ctypes.c_int),
             "ttsh_format_conf": ([ctypes.c_int, ctypes.c_int, _D, _D, _D, ctypes.c_char_p], ctypes.c_int),
             "ttsh_destroy": ([_VP], None),
             "ttsh_strerror": ([ctypes.c_int], ctypes.c_char_p),
@@ -287,6 +288,14 @@ class Sim:
         if check or rc != E_UNSTABLE:
             _check(rc)
         return st.as_dict()
+
+    def reduce_all(self, mass_only: bool = False, check: bool = True):
+        """FP64 diagnostics of every droplet (one pass per size group, one copy back)."""
+        arr = (Stats * self.n)()
+        rc = lib().ttsh_reduce_all(self._h, 1 if mass_only else 0, arr)
+        if check or rc != E_UNSTABLE:
+            _check(rc)
+        return [a.as_dict() for a in arr]
 
     def write_conf(self, inst: int, path: str):
         _check(lib().ttsh_write_conf(self._h, inst, path.encode()))

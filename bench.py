@@ -43,15 +43,26 @@ import numpy as np  # noqa: E402
 
 METRIC = "Msite·steps/s at 256³, batched FP32 vs plain FP64 on one GB300; %HBM peak"
 UNIT = "Msite*steps/s"
-# Algorithmic words (one scalar per site) per site-step of each kernel class; 34 in total for
-# the three-phase schedule (fused_rhs 16, the FFT round trip 8 for two scalars, fused_correct 14),
-# B_alg = 136 B in FP32, 272 B in FP64.
+# B_alg: the compulsory traffic of the minimal three-phase schedule, 34 words per site-step
+# (136 B in FP32, 272 B in FP64): the RHS reads phi, P, u (7) and writes phi', u*, P* and the
+# two Poisson sources (9); the FFT moves each source once (2 + 2); the correction reads u*, P*,
+# the two pressures (8) and writes u, P (6). The %HBM of a step uses B_alg.
+# KERNEL_WORDS: the algorithmic words of each kernel of this build (the divergence and every FFT
+# pass are separate launches here), used for the per-kernel roofline.
 B_ALG_WORDS = 34
 KERNEL_WORDS = {
-    "fused_rhs": 16,        # reads phi, P, u (7); writes phi', u*, P* (7) and the packed source (2)
+    "fused_rhs": 16,        # reads phi, P, u (7); writes phi', u*, P* (7); the phi compensation (2)
+    "fused_div": 8,         # reads u*, P* (6); writes the packed source W (2)
     "fused_correct": 14,    # reads u*, P* (6) and the packed pressure (2); writes u, P (6)
-    "stage1": 17, "stage2": 27, "div": 8, "correct": 14,
+    "stage1": 17, "stage2": 27, "div": 8, "correct": 14,  # plain form
     "fft_x_fwd": 4, "fft_y_fwd": 4, "fft_z_poisson": 4, "fft_y_inv": 4, "fft_x_inv": 4,
+}
+
+# DRAM bytes per site of the dominant FP32 kernels, dram__bytes_read.sum + dram__bytes_write.sum
+# of one ncu capture on a 256^3 droplet (--set full, --clock-control none); a launch over more
+# sites scales with the sites (every kernel streams its planes once).
+TRAFFIC_BYTES_PER_SITE_F32 = {
+    "fused_rhs": (557.219328e6 + 497.564672e6) / 256 ** 3,
 }
 
 
@@ -300,6 +311,9 @@ def main():
     dom_name, (dom_ms, dom_launches) = dom
     dom_bytes = KERNEL_WORDS.get(dom_name, 0) * wbytes * sites
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
+    traffic = None
+    if args.precision == 32 and dom_name in TRAFFIC_BYTES_PER_SITE_F32:
+        traffic = TRAFFIC_BYTES_PER_SITE_F32[dom_name] * sites
     launches = sim.launches_per_step()
 
     # end to end through the public API: host state -> device, K steps each followed by the
@@ -316,19 +330,19 @@ def main():
             sim.set_state(i, phi, P, u)
         for _ in range(args.steps):
             sim.step(1)
-            for i in range(len(drops)):
-                sim.reduce(i, check=False)
+            sim.reduce_all(mass_only=True, check=False)
         for i, (phi, P, u) in enumerate(outs):
             lib_rc = ttsh.lib().ttsh_get_state(sim.handle, i, ttsh._p(phi), ttsh._p(P), ttsh._p(u), None, None)
             ttsh._check(lib_rc)
         torch.cuda.synchronize()
         wall = replicas.max_over_ranks(time.perf_counter() - t0, device="cuda")
         h2d = sum(7 * d[0] ** 3 * 8 for d in drops)
-        d2h = args.steps * len(drops) * 4 * 8 * 256 + sum(7 * d[0] ** 3 * 8 for d in drops)
+        d2h = args.steps * len(drops) * 4 * 8 * 256 + sum(7 * d[0] ** 3 * 8 for d in drops)  # partials + state
         e2e = {"value": sites * world * args.steps / wall / 1e6, "unit": UNIT,
                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
                "note": "public API (ttsh.Sim): set_state from pinned host FP64 arrays, %d x (step + FP64 "
-                       "mass/divergence read-back per droplet), get_state of all fields; wall clock" % args.steps}
+                       "mass read-back of every droplet, ttsh_reduce_all), get_state of all fields; wall "
+                       "clock" % args.steps}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -348,7 +362,9 @@ def main():
                 "parallelism": "replicas" if world > 1 else "1 GPU"},
             "hbm_pct_of_step": 100 * hbm_frac,
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "traffic_source": "ncu DRAM read+write bytes of one 256^3 launch, scaled by sites"
+                         if traffic is not None else None,
                          "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
                          peak_kind, "bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms / max(1, dom_launches)},
             "kernels_ms_per_step": {k: round(v[0], 4) for k, v in prof.items()},

@@ -145,6 +145,14 @@ int ttsh_get_provisional(ttsh_sim* s, int inst, double* ustar, double* Pstar);
 /* FP64 diagnostics (new; the reference has none): mass, divergence, non-finite watchdog. */
 int ttsh_reduce(ttsh_sim* s, int inst, ttsh_stats* out);
 
+/* The same diagnostics for every droplet of the handle in one pass per size group and one
+ * device-to-host copy: out[i] for each instance i. TTSH_STATS_MASS computes only the FP64 mass
+ * and the non-finite flag of phi (max_div_u and max_abs_u are set to -1): the per-step monitor of
+ * a batch. TTSH_STATS_ALL is ttsh_reduce for every droplet. */
+#define TTSH_STATS_ALL 0
+#define TTSH_STATS_MASS 1
+int ttsh_reduce_all(ttsh_sim* s, int what, ttsh_stats* out);
+
 /* ExpoConf (TTSH3D.cu:899-1014): write the snapshot text file of instance `inst` at `path`:
  * one line per site, y outer, x, z inner; columns "vx vy vz px py pz phi" printed as
  * fixed with 15 decimals (ExpoData == 1) or "vx vy " (ExpoData == -1). */
@@ -167,7 +175,8 @@ int ttsh_snapshot_slice(ttsh_sim* s, int inst, double* centroid, int* index, dou
  * only vx, vy of InitCond == 0 from data/conf_<t0>.dat). The file holds T and phi, P, u, u*, P*
  * (u*, P* feed the next step's stale halo) as the device stores them (FP32 or FP64), so a run
  * resumed from it continues bit for bit. Layout: "TTSHCKP1", int32 version 1, int32 N, int32
- * precision, int32 0, double T, int64 steps, then 13 arrays of N^3 (phi, P x3, u x3, u* x3, P* x3).
+ * precision, int32 extra, double T, int64 steps, then 13 + extra arrays of N^3 (phi, P x3, u x3,
+ * u* x3, P* x3; the fused FP32 form adds its phi-update compensation, extra = 1).
  * The pressures are not stored: they are recomputed by the next step. */
 int ttsh_save_checkpoint(ttsh_sim* s, int inst, const char* path);
 int ttsh_load_checkpoint(ttsh_sim* s, int inst, const char* path);

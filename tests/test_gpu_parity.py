@@ -138,3 +138,21 @@ def test_fft_kernels_agree(oracle_mod, N, monkeypatch):
     for g in (a, b):
         errs = field_errors(g, o)
         assert max(errs.values()) <= FP64_TOL, errs
+
+
+def test_reduce_all_matches_single_reduce():
+    """ttsh_reduce_all (one pass per size group) equals ttsh_reduce per droplet; mass-only mode too."""
+    import ttsh
+    sizes = [16, 24, 16]
+    states = [random_state(N, seed=50 + i) for i, N in enumerate(sizes)]
+    inps = [ttsh.default_input(Nx=N, Ny=N, Nz=N) for N in sizes]
+    with ttsh.Sim(inps, [ttsh.default_ext(precision=64) for _ in sizes]) as s:
+        for i, st in enumerate(states):
+            s.set_state(i, st["phi"], st["P"], st["u"])
+        s.step(2)
+        one = [s.reduce(i) for i in range(len(sizes))]
+        allf = s.reduce_all()
+        mass = s.reduce_all(mass_only=True)
+    for a, b, m in zip(one, allf, mass):
+        assert a == b
+        assert m["mass"] == a["mass"] and m["nonfinite"] == 0 and m["max_div_u"] == -1.0
