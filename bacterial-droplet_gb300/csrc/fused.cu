@@ -11,11 +11,13 @@
 //
 // All three march along z through a tile of TX x TY columns (a "2.5D" sweep): each z-plane of
 // every field the stencils need is staged once in a shared-memory ring of planes, and each
-// thread evaluates the 27-point derivatives / 15-point Laplacians of a 1 x RY strip of sites
-// from registers (the strip's 3 x (RY+2) x 3 neighbourhood), so warps read shared memory with
+// thread evaluates the 27-point derivatives / 15-point Laplacians of a 1 x R strip of sites
+// from registers (the strip's 3 x (R+2) x 3 neighbourhood), so warps read shared memory with
 // unit stride. The nested stencils of the RHS (sigma and mu need D P and L P; the velocity
-// update needs D sigma and L mu) are staged: the ring of stage-1 products at plane z+1 is built
-// one plane ahead of the plane z whose update reads it.
+// update needs D sigma and L mu) are staged: stage 1 forms the products of plane z+1 while
+// the thread of each tile column finishes plane z. It splits those outer stencils into
+// in-plane partial sums and carries the z-combination in registers from plane to plane,
+// so every product plane is read once.
 //
 // The stencil arithmetic is the reference's (st_dx/st_dy/st_dz/st_lap of common.cuh) in FP32;
 // the stress enters as one field per component, S_ab = cA phi D_a P_b - zeta phi P_a P_b, whose
@@ -34,26 +36,31 @@ constexpr int TX = 32, TY = 16;   // output tile (columns)
 constexpr int ZC = 64;            // z-planes per block (chunk)
 constexpr int RB = 2;             // strip length (sites per thread) of fused_rhs stage 1
 constexpr int NT = 512;           // threads of fused_rhs: one tile column each in stage 2
+constexpr int US = 4;             // strip length of the velocity terms (phase 1)
 
 // fused_rhs regions: A = tile + 2 (phi, P), B = tile + 1 (u, stage-1 products), C = tile.
 constexpr int AW = TX + 4, AH = TY + 4, AN = AW * AH;
 constexpr int BW = TX + 2, BH = TY + 2, BN = BW * BH;
 constexpr int CN = TX * TY;
-// Shared memory (floats): A ring RA planes x 4 fields; u ring RU x 3; B ring 3 planes x 13
-// products; "partials" ring 2 planes x 7 on the tile. The A and u rings hold one plane more than
-// the stencils read: the next plane is copied into it (cp.async) while the current ones compute.
+// stage-1 products of one plane on B, and the pointwise parts of the update ("partials") on C
+constexpr int QS = 0, QMU = 9, QMU0 = 12, NQ = 13;
+constexpr int PU = 0, PP = 3, PPHI = 6;
+// Shared memory (floats): A ring RA planes x 4 fields; u ring RU x 3; one plane of the 13
+// products; partials ring 2 planes x 7. The A and u rings hold one plane more than the stencils
+// read: the next plane is copied into it (cp.async) while the current ones compute.
 constexpr int RA = 4, RU = 4;
 constexpr int SA_OFF = 0;
 constexpr int SU_OFF = SA_OFF + RA * 4 * AN;
 constexpr int SB_OFF = SU_OFF + RU * 3 * BN;
-constexpr int SQ_OFF = SB_OFF + 3 * 13 * BN;
-constexpr int SZ_OFF = SQ_OFF + 2 * 7 * CN;
-// one plane of the stress z-combinations (s_z S_xb, s_z S_yb, delta_z S_zb) for stage 2
-constexpr int RHS_SMEM_FLOATS = SZ_OFF + 9 * BN;
+constexpr int SQ_OFF = SB_OFF + NQ * BN;
+constexpr int RHS_SMEM_FLOATS = SQ_OFF + 2 * 7 * CN;
 constexpr size_t RHS_SMEM = RHS_SMEM_FLOATS * sizeof(float);
-// stage-1 products in the B ring, and the pointwise parts of the update ("partials")
-constexpr int QS = 0, QMU = 9, QMU0 = 12, NQ = 13;
-constexpr int PU = 0, PP = 3, PPHI = 6;
+// phase-1 thread roles of fused_rhs: stage-1 strips of the B region, then the velocity strips
+constexpr int NS1 = (BW * BH) / RB;                   // 306 stage-1 strips
+constexpr int NU0 = ((NS1 + 31) / 32) * 32;           // first velocity thread (warp aligned)
+constexpr int NUS = TX * (TY / US);                   // 128 velocity strips
+static_assert((BH % RB) == 0 && (TY % US) == 0, "strip lengths divide the regions");
+static_assert(NU0 + NUS <= NT, "phase-1 roles fit the block");
 
 __device__ __forceinline__ int wrapN(int a, int N) { return a < 0 ? a + N : (a >= N ? a - N : a); }
 
@@ -180,15 +187,14 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
   float* const phic = I.phic;
   float* sA = sm + SA_OFF;  // [RA][4][AN]: phi, Px, Py, Pz
   float* sU = sm + SU_OFF;  // [RU][3][BN]
-  float* sB = sm + SB_OFF;  // [3][NQ][BN]
+  float* sB = sm + SB_OFF;  // [NQ][BN]: products of plane b
   float* sQ = sm + SQ_OFF;  // [2][7][CN]
-  float* sZ = sm + SZ_OFF;  // [9][BN]: z-combined stress of plane c
   const int tid = threadIdx.x;
   const int niter = (z1 - z0) + 4;
 
   // issue(i): A plane a = z0 - 2 + i (phi, P over tile+2) into A slot i % RA, and u plane a - 1
-  // (tile+1) into u slot i % RU. Iteration i computes stage 1 at plane b = a - 1 and stage 2 at
-  // plane c = a - 2; issue(i + 1) runs during iteration i.
+  // (tile+1) into u slot i % RU. Iteration i runs stage 1 at plane b = a - 1 and finishes plane
+  // c = a - 2; issue(i + 1) runs during iteration i.
   auto issue = [&](int i) {
     const int za = ((z0 - 2 + i) % N + N) % N;
     float* dst = sA + (i % RA) * 4 * AN;
@@ -211,169 +217,192 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
     }
     cp_async_commit();
   };
-  // stage-2 site of this thread (one site per thread of the tile)
+  // the tile column of this thread in phase 2
   const int qx = tid % TX, qy = tid / TX;
   const size_t gc = (size_t)(y0 + qy) * N + (x0 + qx);
+  const int qo = (qy + 1) * BW + (qx + 1);  // its B-region index
+  // z-combinations carried from plane to plane (phase 2): for the Laplacians of mu_b, mu_0,
+  // rL1 = the partial sum of the plane just finished + 1, rL2 = that of the plane after it;
+  // likewise rD1 / rD2 for the stress divergence of column b
+  float rL1[4] = {0.f, 0.f, 0.f, 0.f}, rL2[4] = {0.f, 0.f, 0.f, 0.f};
+  float rD1[3] = {0.f, 0.f, 0.f}, rD2[3] = {0.f, 0.f, 0.f};
   issue(0);
   for (int i = 0; i < niter; ++i) {
     cp_async_wait_all();
     __syncthreads();
     if (i + 1 < niter) issue(i + 1);
-    // the phi compensation of this iteration's stage-2 site, loaded before stage 1 so that the
-    // stage-1 work covers the load
+    // the phi compensation of this iteration's output site, loaded before phase 1 so that the
+    // phase-1 work covers the load
     const float cprev = i >= 4 ? phic[(size_t)(z0 - 4 + i) * NN + gc] : 0.f;
-    // ---- stage 1 at plane b = z0 - 3 + i over B (tile+1): the products mu_0, mu_b, S_ab that
-    //      stage 2 differentiates, and on the tile the pointwise parts of the update
-    if (i >= 2) {
+    // ---- phase 1a, stage 1 at plane b = z0 - 3 + i over B (tile+1): the products mu_0, mu_b,
+    //      S_ab that phase 2 differentiates, and on the tile the pointwise parts of the update
+    if (i >= 2 && tid < NS1) {
       const float* a0 = sA + ((i + RA - 2) % RA) * 4 * AN;  // plane b-1
       const float* a1 = sA + ((i + RA - 1) % RA) * 4 * AN;  // plane b
       const float* a2 = sA + (i % RA) * 4 * AN;             // plane b+1
       const float* ub = sU + (i % RU) * 3 * BN;             // u at plane b
-      float* bq = sB + (i % 3) * NQ * BN;
+      float* bq = sB;
       float* pq = sQ + (i & 1) * 7 * CN;
       // strips of the B region: warps take 32 consecutive columns of one strip row (unit-stride
       // shared-memory access); the last BW - 32 columns of every row come after them
-      constexpr int NSR = BH / RB, NMAIN = 32 * NSR, NEXTRA = (BW - 32) * NSR;
-      for (int s = tid; s < NMAIN + NEXTRA; s += NT) {
-        int bx, by0;
-        if (s < NMAIN) { bx = s & 31; by0 = (s >> 5) * RB; }
-        else { const int e = s - NMAIN; bx = 32 + e % (BW - 32); by0 = (e / (BW - 32)) * RB; }
-        const int ax = bx + 1, ay0 = by0 + 1;  // A coordinates
-        float phc[RB], lphi[RB], dphi[3][RB];
-        {
-          Hood<RB> h;
-          h.load(a0, a1, a2, AW, ax, ay0);
+      constexpr int NSR = BH / RB, NMAIN = 32 * NSR;
+      const int s = tid;
+      int bx, by0;
+      if (s < NMAIN) { bx = s & 31; by0 = (s >> 5) * RB; }
+      else { const int e = s - NMAIN; bx = 32 + e % (BW - 32); by0 = (e / (BW - 32)) * RB; }
+      const int ax = bx + 1, ay0 = by0 + 1;  // A coordinates
+      float phc[RB], lphi[RB], dphi[3][RB];
+      {
+        Hood<RB> h;
+        h.load(a0, a1, a2, AW, ax, ay0);
 #pragma unroll
-          for (int k = 0; k < RB; ++k) phc[k] = h.v[1][1 + k][1];
-          sep_eval<RB, true, true, true, true>(h, sk, dphi[0], dphi[1], dphi[2], lphi);
-        }
-        float Pc[3][RB], DP[3][3][RB];  // DP[a][b] = D_a P_b
+        for (int k = 0; k < RB; ++k) phc[k] = h.v[1][1 + k][1];
+        sep_eval<RB, true, true, true, true>(h, sk, dphi[0], dphi[1], dphi[2], lphi);
+      }
+      float Pc[3][RB], DP[3][3][RB];  // DP[a][b] = D_a P_b
 #pragma unroll
-        for (int b = 0; b < 3; ++b) {
-          Hood<RB> h;
-          h.load(a0 + (1 + b) * AN, a1 + (1 + b) * AN, a2 + (1 + b) * AN, AW, ax, ay0);
-          float lp[RB];
-          sep_eval<RB, true, true, true, true>(h, sk, DP[0][b], DP[1][b], DP[2][b], lp);
-#pragma unroll
-          for (int k = 0; k < RB; ++k) {
-            Pc[b][k] = h.v[1][1 + k][1];
-            bq[(QMU + b) * BN + (by0 + k) * BW + bx] = fmaf(p.La2, lp[k], phc[k] * Pc[b][k]);  // mu_b (:571-573)
-          }
-        }
+      for (int b = 0; b < 3; ++b) {
+        Hood<RB> h;
+        h.load(a0 + (1 + b) * AN, a1 + (1 + b) * AN, a2 + (1 + b) * AN, AW, ax, ay0);
+        float lp[RB];
+        sep_eval<RB, true, true, true, true>(h, sk, DP[0][b], DP[1][b], DP[2][b], lp);
 #pragma unroll
         for (int k = 0; k < RB; ++k) {
-          const float ph = phc[k];
-          const int o = (by0 + k) * BW + bx;
-          const float mu0 = p.aPhi2 * (ph - 3 * ph * ph + 2 * ph * ph * ph) - p.kPhi * lphi[k];  // mu_0 (:567)
-          bq[QMU0 * BN + o] = mu0;
-          const float* bq1 = sB + ((i + 2) % 3) * NQ * BN;  // plane b-1 (this thread's own column)
-          const float* bq2 = sB + ((i + 1) % 3) * NQ * BN;  // plane b-2
+          Pc[b][k] = h.v[1][1 + k][1];
+          bq[(QMU + b) * BN + (by0 + k) * BW + bx] = fmaf(p.La2, lp[k], phc[k] * Pc[b][k]);  // mu_b (:571-573)
+        }
+      }
 #pragma unroll
-          for (int a = 0; a < 3; ++a)
+      for (int k = 0; k < RB; ++k) {
+        const float ph = phc[k];
+        const int o = (by0 + k) * BW + bx;
+        const float mu0 = p.aPhi2 * (ph - 3 * ph * ph + 2 * ph * ph * ph) - p.kPhi * lphi[k];  // mu_0 (:567)
+        bq[QMU0 * BN + o] = mu0;
 #pragma unroll
-            for (int b = 0; b < 3; ++b) {
-              float sv = p.cA * (ph * DP[a][b][k]);  // cA * sigma_ab (:587-595)
-              if (p.zeta != 0.f) sv -= p.zeta * (ph * Pc[a][k] * Pc[b][k]);
-              bq[(QS + a * 3 + b) * BN + o] = sv;
-              // z-combination at plane b-1 of the stress component the divergence needs along a:
-              // s_z for a = x, y and delta_z for a = z (planes b-2, b-1, b of this column)
-              const float s2 = bq2[(QS + a * 3 + b) * BN + o], s1 = bq1[(QS + a * 3 + b) * BN + o];
-              sZ[(a * 3 + b) * BN + o] = a < 2 ? fmaf(4.f, s1, s2 + sv) : sv - s2;
-            }
-          const int cx = bx - 1, cy = by0 + k - 1;
-          if (cx >= 0 && cx < TX && cy >= 0 && cy < TY) {
-            // pointwise parts of getDtF (:617-631) at this site of plane b
-            const int c = cy * TX + cx;
-            const float vx = ub[o], vy = ub[BN + o], vz = ub[2 * BN + o];
-            const float px = Pc[0][k], py = Pc[1][k], pz = Pc[2][k];
-            const float P2 = px * px + py * py + pz * pz;
-            const float dPhi2 = dphi[0][k] * dphi[0][k] + dphi[1][k] * dphi[1][k] + dphi[2][k] * dphi[2][k];
+        for (int a = 0; a < 3; ++a)
 #pragma unroll
-            for (int b = 0; b < 3; ++b) {
-              pq[(PU + b) * CN + c] = mu0 * dphi[b][k];  // mu_0 D_b phi
-              const float pb = Pc[b][k];
-              float cub;
-              if (b == 0) cub = px * px * px + px * py * py + px * pz * pz;
-              else if (b == 1) cub = px * py * px + py * py * py + py * pz * pz;
-              else cub = px * pz * px + py * pz * py + pz * pz * pz;
-              const float Ab = dphi[0][k] * dphi[b][k] * px + dphi[1][k] * dphi[b][k] * py + dphi[2][k] * dphi[b][k] * pz;
-              pq[(PP + b) * CN + c] = -vx * DP[0][b][k] - vy * DP[1][b][k] - vz * DP[2][b][k] - p.alpha * ph * pb -
-                                      p.beta * P2 * pb - p.lambda0 * (px * DP[0][b][k] + py * DP[1][b][k] + pz * DP[2][b][k]) -
-                                      p.A * (dPhi2 * cub + sqrtf(P2) * Ab);
-            }
-            pq[PPHI * CN + c] = -vx * dphi[0][k] - vy * dphi[1][k] - vz * dphi[2][k];
+          for (int b = 0; b < 3; ++b) {
+            float sv = p.cA * (ph * DP[a][b][k]);  // cA * sigma_ab (:587-595)
+            if (p.zeta != 0.f) sv -= p.zeta * (ph * Pc[a][k] * Pc[b][k]);
+            bq[(QS + a * 3 + b) * BN + o] = sv;
           }
+        const int cx = bx - 1, cy = by0 + k - 1;
+        if (cx >= 0 && cx < TX && cy >= 0 && cy < TY) {
+          // pointwise parts of getDtF (:617-631) at this site of plane b
+          const int c = cy * TX + cx;
+          const float vx = ub[o], vy = ub[BN + o], vz = ub[2 * BN + o];
+          const float px = Pc[0][k], py = Pc[1][k], pz = Pc[2][k];
+          const float P2 = px * px + py * py + pz * pz;
+          const float dPhi2 = dphi[0][k] * dphi[0][k] + dphi[1][k] * dphi[1][k] + dphi[2][k] * dphi[2][k];
+#pragma unroll
+          for (int b = 0; b < 3; ++b) {
+            pq[(PU + b) * CN + c] = mu0 * dphi[b][k];  // mu_0 D_b phi
+            const float pb = Pc[b][k];
+            float cub;
+            if (b == 0) cub = px * px * px + px * py * py + px * pz * pz;
+            else if (b == 1) cub = px * py * px + py * py * py + py * pz * pz;
+            else cub = px * pz * px + py * pz * py + pz * pz * pz;
+            const float Ab = dphi[0][k] * dphi[b][k] * px + dphi[1][k] * dphi[b][k] * py + dphi[2][k] * dphi[b][k] * pz;
+            pq[(PP + b) * CN + c] = -vx * DP[0][b][k] - vy * DP[1][b][k] - vz * DP[2][b][k] - p.alpha * ph * pb -
+                                    p.beta * P2 * pb - p.lambda0 * (px * DP[0][b][k] + py * DP[1][b][k] + pz * DP[2][b][k]) -
+                                    p.A * (dPhi2 * cub + sqrtf(P2) * Ab);
+          }
+          pq[PPHI * CN + c] = -vx * dphi[0][k] - vy * dphi[1][k] - vz * dphi[2][k];
         }
       }
     }
-    __syncthreads();
-    // ---- stage 2 at plane c = z0 - 4 + i on the tile: u*, P*, phi'
-    if (i >= 4) {
-      const int zc = z0 - 4 + i;
+    // ---- phase 1b, on the threads stage 1 leaves free: the velocity terms of plane c = b - 1,
+    //      -u.D u_b + mu L u_b (:617-621), added to that plane's partials (written by stage 1 at
+    //      iteration i - 1), for a strip of US sites of one tile column
+    if (i >= 4 && tid >= NU0 && tid < NU0 + NUS) {
+      const int s = tid - NU0;
+      const int vx = s & 31, vy0 = (s >> 5) * US;  // tile coordinates of the strip
       const float* u0 = sU + ((i + RU - 2) % RU) * 3 * BN;  // plane c-1
       const float* u1 = sU + ((i + RU - 1) % RU) * 3 * BN;  // plane c
       const float* u2 = sU + (i % RU) * 3 * BN;             // plane c+1
-      const float* q0 = sB + ((i + 1) % 3) * NQ * BN;
-      const float* q1 = sB + ((i + 2) % 3) * NQ * BN;
-      const float* q2 = sB + (i % 3) * NQ * BN;
-      const float* pq = sQ + ((i + 1) & 1) * 7 * CN;        // written at iteration i - 1
-      const float* ac = sA + ((i + RA - 2) % RA) * 4 * AN;   // phi, P at plane c
-      const int bx = qx + 1, by = qy + 1;
-      const int c = qy * TX + qx, oa = (qy + 2) * AW + (qx + 2);
-      const size_t g = (size_t)zc * NN + gc;
-      float uc[3], du[3][3], lu[3];  // du[b][a] = D_a u_b
+      float* pq = sQ + ((i + 1) & 1) * 7 * CN;
+      float uc[3][US];
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+#pragma unroll
+        for (int k = 0; k < US; ++k) uc[b][k] = u1[b * BN + (vy0 + 1 + k) * BW + vx + 1];
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
-        Hood<1> h;
-        h.load(u0 + b * BN, u1 + b * BN, u2 + b * BN, BW, bx, by);
-        uc[b] = h.v[1][1][1];
-        sep_eval<1, true, true, true, true>(h, sk, &du[b][0], &du[b][1], &du[b][2], &lu[b]);
-      }
-      // velocity: d/dt u_b (:617-621) + the stress divergence; u*_b = u_b + dt d/dt u_b (:480-482)
-#pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        // divergence of stress column b from the z-combined plane: delta_x s_y, s_x delta_y, s_x s_y
-        float fx, fy, fz;
+        float dx[US], dy[US], dz[US], lu[US];
         {
-          const float* Z1 = sZ + (0 * 3 + b) * BN;
-          const float* Z2 = sZ + (1 * 3 + b) * BN;
-          const float* Z3 = sZ + (2 * 3 + b) * BN;
-          const int o = by * BW + bx;
-          auto sy = [&](const float* Z, int dx) { return fmaf(4.f, Z[o + dx], Z[o + dx - BW] + Z[o + dx + BW]); };
-          auto dy = [&](const float* Z, int dx) { return Z[o + dx + BW] - Z[o + dx - BW]; };
-          fx = sk.d * (sy(Z1, 1) - sy(Z1, -1));
-          fy = sk.d * fmaf(4.f, dy(Z2, 0), dy(Z2, -1) + dy(Z2, 1));
-          fz = sk.d * fmaf(4.f, sy(Z3, 0), sy(Z3, -1) + sy(Z3, 1));
+          Hood<US> h;
+          h.load(u0 + b * BN, u1 + b * BN, u2 + b * BN, BW, vx + 1, vy0 + 1);
+          sep_eval<US, true, true, true, true>(h, sk, dx, dy, dz, lu);
         }
-        const float r = -uc[0] * du[b][0] - uc[1] * du[b][1] - uc[2] * du[b][2] + p.mu * lu[b] +
-                        pq[(PU + b) * CN + c] + (fx + fy + fz);
-        oUs[b][g] = uc[b] + p.dt * r;
+#pragma unroll
+        for (int k = 0; k < US; ++k)
+          pq[(PU + b) * CN + (vy0 + k) * TX + vx] +=
+              -uc[0][k] * dx[k] - uc[1][k] * dy[k] - uc[2][k] * dz[k] + p.mu * lu[k];
       }
-      // polarisation: d/dt P_b = (pointwise part) + eta L mu_b (:623-629); P*_b (:486-488)
+    }
+    __syncthreads();
+    // ---- phase 2, one tile column per thread: the in-plane partial sums of the outer stencils
+    //      over the products of plane b, carried in z; plane c = b - 1 is then complete
+    if (i >= 2) {
+      const float* bq = sB + qo;
+      // 15-point Laplacian L = l12 (8 corners) + l23 (6 faces) - l143 (centre) (:3328-3343):
+      // an off-centre plane p adds G_p = l12 (its 4 diagonal sites) + l23 (its centre site),
+      // the centre plane adds H_p = l23 (its 4 edge sites) - l143 (its centre site)
+      float lmu[4];
+#pragma unroll
+      for (int f = 0; f < 4; ++f) {
+        const float* F = bq + (QMU + f) * BN;
+        const float v11 = F[0];
+        const float dg = (F[-BW - 1] + F[-BW + 1]) + (F[BW - 1] + F[BW + 1]);
+        const float ed = (F[-BW] + F[BW]) + (F[-1] + F[1]);
+        const float G = fmaf(sk.l12, dg, sk.l23 * v11);
+        const float H = fmaf(sk.l23, ed, -sk.l143 * v11);
+        lmu[f] = rL1[f] + G;
+        rL1[f] = rL2[f] + H;
+        rL2[f] = G;
+      }
+      // divergence of stress column b, d/36 (delta_x s_y s_z S_xb + s_x delta_y s_z S_yb +
+      // s_x s_y delta_z S_zb): the plane adds Q = delta_x s_y S_xb + s_x delta_y S_yb with weight
+      // s_z = (1, 4, 1) and Z = s_x s_y S_zb with weight delta_z = (-1, 0, 1) over planes c-1, c, c+1
+      float dv[3];
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
-        float lmu;
-        {
-          Hood<1> h;
-          h.load(q0 + (QMU + b) * BN, q1 + (QMU + b) * BN, q2 + (QMU + b) * BN, BW, bx, by);
-          sep_eval<1, false, false, false, true>(h, sk, nullptr, nullptr, nullptr, &lmu);
-        }
-        oPs[b][g] = ac[(1 + b) * AN + oa] + p.dt * (pq[(PP + b) * CN + c] + p.eta * lmu);
+        const float* X = bq + (QS + 0 * 3 + b) * BN;
+        const float* Y = bq + (QS + 1 * 3 + b) * BN;
+        const float* Z = bq + (QS + 2 * 3 + b) * BN;
+        const float xr = fmaf(4.f, X[1], X[-BW + 1] + X[BW + 1]) - fmaf(4.f, X[-1], X[-BW - 1] + X[BW - 1]);
+        const float yr = fmaf(4.f, Y[BW] - Y[-BW], (Y[BW - 1] - Y[-BW - 1]) + (Y[BW + 1] - Y[-BW + 1]));
+        const float t0 = fmaf(4.f, Z[-1], Z[-BW - 1] + Z[BW - 1]);
+        const float t1 = fmaf(4.f, Z[0], Z[-BW] + Z[BW]);
+        const float t2 = fmaf(4.f, Z[1], Z[-BW + 1] + Z[BW + 1]);
+        const float zr = fmaf(4.f, t1, t0 + t2);
+        const float Q = xr + yr;
+        dv[b] = sk.d * (rD1[b] + Q + zr);
+        rD1[b] = fmaf(4.f, Q, rD2[b]);
+        rD2[b] = Q - zr;
       }
-      // phi: d/dt phi = -u.D phi + gamma L mu_0 (:631); phi' = phi + dt d/dt phi (:515)
-      float lmu0;
-      {
-        Hood<1> h;
-        h.load(q0 + QMU0 * BN, q1 + QMU0 * BN, q2 + QMU0 * BN, BW, bx, by);
-        sep_eval<1, false, false, false, true>(h, sk, nullptr, nullptr, nullptr, &lmu0);
+      if (i >= 4) {
+        const int zc = z0 - 4 + i;
+        const float* pq = sQ + ((i + 1) & 1) * 7 * CN;        // plane c, stage 1 + velocity terms
+        const float* uc = sU + ((i + RU - 1) % RU) * 3 * BN;  // u at plane c
+        const float* ac = sA + ((i + RA - 2) % RA) * 4 * AN;  // phi, P at plane c
+        const int c = qy * TX + qx, oa = (qy + 2) * AW + (qx + 2);
+        const size_t g = (size_t)zc * NN + gc;
+        // u*_b = u_b + dt d/dt u_b (:480-482)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) oUs[b][g] = uc[b * BN + qo] + p.dt * (pq[(PU + b) * CN + c] + dv[b]);
+        // P*_b = P_b + dt (pointwise part + eta L mu_b) (:623-629, :486-488)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) oPs[b][g] = ac[(1 + b) * AN + oa] + p.dt * (pq[(PP + b) * CN + c] + p.eta * lmu[b]);
+        // phi' = phi + dt (-u.D phi + gamma L mu_0) (:631, :515), compensated: the part of the
+        // increment that rounding drops from phi is carried to the next step (otherwise
+        // increments below half an ulp of phi are lost, a systematic mass drift)
+        const float ph = ac[oa];
+        const float inc = fmaf(p.dt, pq[PPHI * CN + c] + p.gamma * lmu[3], cprev);
+        const float nv = ph + inc;
+        phic[g] = inc - (nv - ph);
+        ophi[g] = nv;
       }
-      // compensated update: the part of dt*dphi/dt that rounding drops from phi is carried to the
-      // next step (otherwise increments below half an ulp of phi are lost, a systematic mass drift)
-      const float ph = ac[oa];
-      const float inc = fmaf(p.dt, pq[PPHI * CN + c] + p.gamma * lmu0, cprev);
-      const float nv = ph + inc;
-      phic[g] = inc - (nv - ph);
-      ophi[g] = nv;
     }
   }
 }
