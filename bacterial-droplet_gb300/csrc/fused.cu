@@ -408,19 +408,36 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
 }
 
 // ------------------------------------------------------------------------------------------
-// fused_div / fused_correct: one ring of 3 planes over tile+1, strips of RD sites.
-constexpr int RD = 2;
-constexpr int NTD = TX * TY / RD;  // 256 threads
-constexpr int DN = (TX + 2) * (TY + 2);
-constexpr int RR = 4;  // ring planes of fused_div / fused_correct (3 read + 1 in flight)
-constexpr size_t DIV_SMEM = RR * 6 * DN * sizeof(float);
-constexpr size_t COR_SMEM = RR * DN * sizeof(float2) + 3 * 6 * TX * TY * sizeof(float);
+// fused_div / fused_correct: one tile column per thread; each staged plane is read once, its
+// in-plane partial sums carried in z (as in fused_rhs phase 2), so the ring only has to cover
+// the copies in flight: DR slots, the plane read and DR - 1 planes in flight. Rows are staged in
+// 16-byte chunks: a row starts at a multiple of 4 floats (2 float2) left of the tile, so every
+// chunk, wrapped or not, is one aligned 16-byte global segment (N is a multiple of 32).
+constexpr int NTC = TX * TY;            // 512 threads
+constexpr int SH = TY + 2;              // staged rows y0 - 1 .. y0 + TY
+constexpr int SW = TX + 8;              // fused_div row, floats x0 - 4 .. x0 + TX + 3
+constexpr int SPL = SW * SH;            // floats per staged plane of one field
+constexpr int CW = TX + 4;              // fused_correct row, float2 x0 - 2 .. x0 + TX + 1
+constexpr int CPL = CW * SH;            // float2 per staged plane
+constexpr int DR = 4;                   // ring slots of fused_div / fused_correct
+constexpr size_t DIV_SMEM = DR * 6 * SPL * sizeof(float);
+constexpr size_t COR_SLOT = CPL * sizeof(float2) + 6 * CN * sizeof(float);  // p_v, p_p on B; u*, P* on C
+constexpr size_t COR_SMEM = DR * COR_SLOT;
 
-__global__ void __launch_bounds__(NTD, 3) k_fused_div(const InstDev<float>* __restrict__ insts, int par, int nchunk) {
+// wait until at most DR - 2 copy groups are pending: the group of the plane read now is complete
+__device__ __forceinline__ void cp_async_wait_ring() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(DR - 2) : "memory");
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
+__global__ void __launch_bounds__(NTC, 2) k_fused_div(const InstDev<float>* __restrict__ insts, int par, int nchunk) {
   extern __shared__ __align__(16) float sm[];
   const int N = insts[0].N;
   const InstDev<float>& I = insts[blockIdx.z / nchunk];
-  const Phys<float> p = I.ph;  // by value: read once, kept in registers
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const int z0 = (blockIdx.z % nchunk) * ZC, z1 = min(z0 + ZC, N);
   const size_t NN = (size_t)N * N;
@@ -429,143 +446,150 @@ __global__ void __launch_bounds__(NTD, 3) k_fused_div(const InstDev<float>* __re
   const float* old[6] = {I.Us[par][0], I.Us[par][1], I.Us[par][2], I.Ps[par][0], I.Ps[par][1], I.Ps[par][2]};
   float2* const oW = I.W;
   const int stale_q2 = I.stale;
-  const int W = TX + 2;
+  const float kd = I.ph.c2h * (1.f / 36.f) * I.ph.inv_dt;  // d/36 of the 27-point D, and 1/dt
+  const int tid = threadIdx.x;
   const int niter = (z1 - z0) + 2;
-  // plane z0 - 1 + i into slot i % RR, issued one iteration ahead
+  // issue(i): plane z0 - 1 + i into slot i % DR (an empty group past the last plane, so that
+  // every iteration commits one). Chunks outside the domain come from the previous step's u*, P*
+  // when the stale-halo quirk is on (the chunk grid is aligned with 0 and N).
   auto issue = [&](int i) {
+    if (i >= niter) { cp_async_commit(); return; }
     const int zu = z0 - 1 + i;
     const bool zw = zu < 0 || zu >= N;
     const int zz = wrapN(zu, N);
-    float* dst = sm + (i % RR) * 6 * DN;
-    for (int t = threadIdx.x; t < DN; t += NTD) {
-      const int ry = t / W, rx = t - ry * W;
-      const int gx = x0 - 1 + rx, gy = y0 - 1 + ry;
+    float* dst = sm + (i % DR) * 6 * SPL;
+    constexpr int CR = SW / 4;  // chunks per row
+    for (int t = tid; t < SH * CR; t += NTC) {
+      const int ry = t / CR, rc = t - ry * CR;
+      const int gx = x0 - 4 + 4 * rc, gy = y0 - 1 + ry;
       const bool stale = stale_q2 && (zw || gx < 0 || gx >= N || gy < 0 || gy >= N);
       const size_t g = (size_t)zz * NN + (size_t)wrapN(gy, N) * N + wrapN(gx, N);
 #pragma unroll
-      for (int f = 0; f < 6; ++f) cp_async4(dst + f * DN + t, (stale ? old[f] : cur[f]) + g);
+      for (int f = 0; f < 6; ++f) cp_async16(dst + f * SPL + ry * SW + 4 * rc, (stale ? old[f] : cur[f]) + g);
     }
     cp_async_commit();
   };
-  issue(0);
+  const int qx = tid % TX, qy = tid / TX;
+  const size_t gc = (size_t)(y0 + qy) * N + (x0 + qx);
+  // the divergence D_x v_x + D_y v_y + D_z v_z of v = u*, P* (getStream mode 0, :664-670), each
+  // D = d/36 delta s s: a plane adds Q = delta_x s_y v_x + s_x delta_y v_y with weight s_z =
+  // (1, 4, 1) and Z = s_x s_y v_z with weight delta_z = (-1, 0, 1) over planes c-1, c, c+1
+  float rD1[2] = {0.f, 0.f}, rD2[2] = {0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < DR - 1; ++k) issue(k);
   for (int i = 0; i < niter; ++i) {
-    cp_async_wait_all();
+    cp_async_wait_ring();
     __syncthreads();
-    if (i + 1 < niter) issue(i + 1);
-    if (i >= 2) {
-      const int zc = z0 - 2 + i;
-      const float* s0 = sm + ((i + RR - 2) % RR) * 6 * DN;
-      const float* s1 = sm + ((i + RR - 1) % RR) * 6 * DN;
-      const float* s2 = sm + (i % RR) * 6 * DN;
-      const int cx = threadIdx.x % TX, cy0 = (threadIdx.x / TX) * RD;
-      float d[2][RD];
-      const SepK sk{p.c2h * (1.f / 36.f), p.cl12, p.cl23, p.cl143};
+    issue(i + DR - 1);  // into the slot read at iteration i - 1
+    const float* s = sm + (i % DR) * 6 * SPL + (qy + 1) * SW + (qx + 4);
+    float dv[2];
 #pragma unroll
-      for (int f = 0; f < 2; ++f) {
-        float gx[RD], gy[RD], gz[RD];
-        {
-          Hood<RD> h;
-          h.load(s0 + (3 * f + 0) * DN, s1 + (3 * f + 0) * DN, s2 + (3 * f + 0) * DN, W, cx + 1, cy0 + 1);
-          sep_eval<RD, true, false, false, false>(h, sk, gx, nullptr, nullptr, nullptr);
-        }
-        {
-          Hood<RD> h;
-          h.load(s0 + (3 * f + 1) * DN, s1 + (3 * f + 1) * DN, s2 + (3 * f + 1) * DN, W, cx + 1, cy0 + 1);
-          sep_eval<RD, false, true, false, false>(h, sk, nullptr, gy, nullptr, nullptr);
-        }
-        {
-          Hood<RD> h;
-          h.load(s0 + (3 * f + 2) * DN, s1 + (3 * f + 2) * DN, s2 + (3 * f + 2) * DN, W, cx + 1, cy0 + 1);
-          sep_eval<RD, false, false, true, false>(h, sk, nullptr, nullptr, gz, nullptr);
-        }
-#pragma unroll
-        for (int k = 0; k < RD; ++k) d[f][k] = (gx[k] + gy[k] + gz[k]) * p.inv_dt;
-      }
-#pragma unroll
-      for (int k = 0; k < RD; ++k) {
-        const size_t g = (size_t)zc * NN + (size_t)(y0 + cy0 + k) * N + (x0 + cx);
-        oW[g] = make_float2(d[0][k], d[1][k]);
-      }
+    for (int f = 0; f < 2; ++f) {
+      const float* X = s + (3 * f + 0) * SPL;
+      const float* Y = s + (3 * f + 1) * SPL;
+      const float* Z = s + (3 * f + 2) * SPL;
+      const float xr = fmaf(4.f, X[1], X[-SW + 1] + X[SW + 1]) - fmaf(4.f, X[-1], X[-SW - 1] + X[SW - 1]);
+      const float yr = fmaf(4.f, Y[SW] - Y[-SW], (Y[SW - 1] - Y[-SW - 1]) + (Y[SW + 1] - Y[-SW + 1]));
+      const float t0 = fmaf(4.f, Z[-1], Z[-SW - 1] + Z[SW - 1]);
+      const float t1 = fmaf(4.f, Z[0], Z[-SW] + Z[SW]);
+      const float t2 = fmaf(4.f, Z[1], Z[-SW + 1] + Z[SW + 1]);
+      const float zr = fmaf(4.f, t1, t0 + t2);
+      const float Q = xr + yr;
+      dv[f] = rD1[f] + Q + zr;
+      rD1[f] = fmaf(4.f, Q, rD2[f]);
+      rD2[f] = Q - zr;
     }
+    if (i >= 2) oW[(size_t)(z0 - 2 + i) * NN + gc] = make_float2(kd * dv[0], kd * dv[1]);
   }
 }
 
-__global__ void __launch_bounds__(NTD, 3) k_fused_correct(const InstDev<float>* __restrict__ insts, int par, int nchunk) {
-  extern __shared__ __align__(16) float2 sm2[];
-  float* sq = reinterpret_cast<float*>(sm2 + RR * DN);  // [3][6][TX*TY]: u*, P* of the compute planes
+__global__ void __launch_bounds__(NTC, 2) k_fused_correct(const InstDev<float>* __restrict__ insts, int par, int nchunk) {
+  extern __shared__ __align__(16) unsigned char smc[];
   const int N = insts[0].N;
   const InstDev<float>& I = insts[blockIdx.z / nchunk];
-  const Phys<float> p = I.ph;  // by value: read once, kept in registers
+  const float kd = I.ph.c2h * (1.f / 36.f);
+  const float dt = I.ph.dt;
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const int z0 = (blockIdx.z % nchunk) * ZC, z1 = min(z0 + ZC, N);
   const size_t NN = (size_t)N * N;
-  const int W = TX + 2;
   const int niter = (z1 - z0) + 2;
   const float* qs[6] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2],
                         I.Ps[par ^ 1][0], I.Ps[par ^ 1][1], I.Ps[par ^ 1][2]};
   float* const oU[3] = {I.U[0], I.U[1], I.U[2]};
   float* const oP[3] = {I.P[0], I.P[1], I.P[2]};
   const float2* __restrict__ gW = I.W;
-  // issue(i): W plane z0 - 1 + i into ring slot i % RR, and u*, P* of plane z0 - 1 + i (computed at
-  // iteration i + 1) into slot i % 3. issue(i + 1) runs during iteration i, while iteration i reads
-  // the u*, P* slot (i - 1) % 3 and issue(i) has filled slot i % 3.
+  const int tid = threadIdx.x;
+  auto slot_w = [&](int i) { return reinterpret_cast<float2*>(smc + (i % DR) * COR_SLOT); };
+  auto slot_q = [&](int i) { return reinterpret_cast<float*>(smc + (i % DR) * COR_SLOT + CPL * sizeof(float2)); };
+  // issue(i): into slot i % DR the pressures (p_v, p_p) of plane z0 - 1 + i over tile+1 and u*, P*
+  // of plane z0 - 2 + i (finished at iteration i) over the tile; an empty group past the last plane
   auto issue = [&](int i) {
-    const int zz = ((z0 - 1 + i) % N + N) % N;
-    float2* dst = sm2 + (i % RR) * DN;
-    for (int t = threadIdx.x; t < DN; t += NTD) {
-      const int ry = t / W, rx = t - ry * W;
-      cp_async8(dst + t, gW + (size_t)zz * NN + (size_t)wrapN(y0 - 1 + ry, N) * N + wrapN(x0 - 1 + rx, N));
+    if (i >= niter) { cp_async_commit(); return; }
+    const int zz = wrapN(z0 - 1 + i, N);
+    float2* dst = slot_w(i);
+    constexpr int CR = CW / 2;  // chunks per row
+    for (int t = tid; t < SH * CR; t += NTC) {
+      const int ry = t / CR, rc = t - ry * CR;
+      cp_async16(dst + ry * CW + 2 * rc,
+                 gW + (size_t)zz * NN + (size_t)wrapN(y0 - 1 + ry, N) * N + wrapN(x0 - 2 + 2 * rc, N));
     }
-    const int zq = z0 - 1 + i;
-    if (zq >= z0 && zq < z1) {
-      float* dq = sq + (i % 3) * 6 * TX * TY;
-      for (int t = threadIdx.x; t < TX * TY; t += NTD) {
-        const int cy = t / TX, cx = t - cy * TX;
-        const size_t g = (size_t)zq * NN + (size_t)(y0 + cy) * N + (x0 + cx);
+    const int zq = z0 - 2 + i;
+    if (zq >= z0) {
+      float* dq = slot_q(i);
+      // 4 groups of TY * TX / 4 threads, one chunk of a tile row each: group k copies fields k, k + 4
+      constexpr int QR = TX / 4, QG = TY * QR;  // chunks per tile row, per field
+      static_assert(4 * QG == NTC, "chunk groups cover the block");
+      const int r = tid % QG, fg = tid / QG;
+      const int ry = r / QR, rc = r - ry * QR;
+      const size_t go = (size_t)zq * NN + (size_t)(y0 + ry) * N + x0 + 4 * rc;
 #pragma unroll
-        for (int f = 0; f < 6; ++f) cp_async4(dq + f * TX * TY + t, qs[f] + g);
-      }
+      for (int f = 0; f < 6; ++f)
+        if ((f & 3) == fg) cp_async16(dq + f * CN + ry * TX + 4 * rc, qs[f] + go);
     }
     cp_async_commit();
   };
-  issue(0);
+  const int qx = tid % TX, qy = tid / TX;
+  const size_t gc = (size_t)(y0 + qy) * N + (x0 + qx);
+  // gradients D_a of p_v and p_p, D = d/36 delta s s: a plane adds X = delta_x s_y p and
+  // Y = s_x delta_y p with weight s_z = (1, 4, 1), Z = s_x s_y p with weight delta_z = (-1, 0, 1)
+  float2 rX1 = make_float2(0.f, 0.f), rX2 = rX1, rY1 = rX1, rY2 = rX1, rZ1 = rX1, rZ2 = rX1;
+#pragma unroll
+  for (int k = 0; k < DR - 1; ++k) issue(k);
   for (int i = 0; i < niter; ++i) {
-    cp_async_wait_all();
+    cp_async_wait_ring();
     __syncthreads();
-    if (i + 1 < niter) issue(i + 1);
+    issue(i + DR - 1);  // into the slot read at iteration i - 1
+    const float2* s = slot_w(i) + (qy + 1) * CW + (qx + 2);
+    float2 v[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) v[r][c] = s[(r - 1) * CW + (c - 1)];
+    float2 gx, gy, gz;
+#define TTSH_PLANE(C)                                                                                          \
+    {                                                                                                          \
+      const float X = fmaf(4.f, v[1][2].C - v[1][0].C, (v[0][2].C - v[0][0].C) + (v[2][2].C - v[2][0].C));     \
+      const float Y = fmaf(4.f, v[2][1].C - v[0][1].C, (v[2][0].C - v[0][0].C) + (v[2][2].C - v[0][2].C));     \
+      const float t0 = fmaf(4.f, v[1][0].C, v[0][0].C + v[2][0].C);                                            \
+      const float t1 = fmaf(4.f, v[1][1].C, v[0][1].C + v[2][1].C);                                            \
+      const float t2 = fmaf(4.f, v[1][2].C, v[0][2].C + v[2][2].C);                                            \
+      const float Z = fmaf(4.f, t1, t0 + t2);                                                                  \
+      gx.C = rX1.C + X; rX1.C = fmaf(4.f, X, rX2.C); rX2.C = X;                                                \
+      gy.C = rY1.C + Y; rY1.C = fmaf(4.f, Y, rY2.C); rY2.C = Y;                                                \
+      gz.C = rZ1.C + Z; rZ1.C = rZ2.C; rZ2.C = -Z;                                                             \
+    }
+    TTSH_PLANE(x)
+    TTSH_PLANE(y)
+#undef TTSH_PLANE
     if (i >= 2) {
-      const int zc = z0 - 2 + i;
-      const int cx = threadIdx.x % TX, cy0 = (threadIdx.x / TX) * RD;
-      const float* dq = sq + ((i + 2) % 3) * 6 * TX * TY;  // staged by issue(i - 1)
-      float gv[3][RD], gp[3][RD];
-      {
-        const SepK sk{p.c2h * (1.f / 36.f), p.cl12, p.cl23, p.cl143};
-        Hood2<RD> h2;
-        h2.load(sm2 + ((i + RR - 2) % RR) * DN, sm2 + ((i + RR - 1) % RR) * DN, sm2 + (i % RR) * DN, W, cx + 1,
-                cy0 + 1);
-        Hood<RD> hv, hp;
+      // getVNew (TTSH3D.cu:505-511): u = u* - dt D p_v, P = P* - dt D p_p
+      const size_t g = (size_t)(z0 - 2 + i) * NN + gc;
+      const float* qc = slot_q(i) + qy * TX + qx;
+      const float gv[3] = {gx.x, gy.x, gz.x}, gp[3] = {gx.y, gy.y, gz.y};
 #pragma unroll
-        for (int z = 0; z < 3; ++z)
-#pragma unroll
-          for (int r = 0; r < RD + 2; ++r)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              hv.v[z][r][c] = h2.v[z][r][c].x;
-              hp.v[z][r][c] = h2.v[z][r][c].y;
-            }
-        sep_eval<RD, true, true, true, false>(hv, sk, gv[0], gv[1], gv[2], nullptr);
-        sep_eval<RD, true, true, true, false>(hp, sk, gp[0], gp[1], gp[2], nullptr);
-      }
-#pragma unroll
-      for (int k = 0; k < RD; ++k) {
-        const int c = (cy0 + k) * TX + cx;
-        const size_t g = (size_t)zc * NN + (size_t)(y0 + cy0 + k) * N + (x0 + cx);
-        // getVNew (TTSH3D.cu:505-511)
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-          oU[b][g] = dq[b * TX * TY + c] - p.dt * gv[b][k];
-          oP[b][g] = dq[(3 + b) * TX * TY + c] - p.dt * gp[b][k];
-        }
+      for (int b = 0; b < 3; ++b) {
+        oU[b][g] = qc[b * CN] - dt * (kd * gv[b]);
+        oP[b][g] = qc[(3 + b) * CN] - dt * (kd * gp[b]);
       }
     }
   }
@@ -604,14 +628,14 @@ void launch_fused_rhs(const Group<float>& g, int par, cudaStream_t st) {
 void launch_fused_div(const Group<float>& g, int par, cudaStream_t st) {
   int nchunk;
   dim3 grid = grid_for(g, nchunk);
-  k_fused_div<<<grid, NTD, DIV_SMEM, st>>>(g.d_inst, par, nchunk);
+  k_fused_div<<<grid, NTC, DIV_SMEM, st>>>(g.d_inst, par, nchunk);
   check(cudaGetLastError(), "fused_div launch");
 }
 
 void launch_fused_correct(const Group<float>& g, int par, cudaStream_t st) {
   int nchunk;
   dim3 grid = grid_for(g, nchunk);
-  k_fused_correct<<<grid, NTD, COR_SMEM, st>>>(g.d_inst, par, nchunk);
+  k_fused_correct<<<grid, NTC, COR_SMEM, st>>>(g.d_inst, par, nchunk);
   check(cudaGetLastError(), "fused_correct launch");
 }
 
