@@ -4,7 +4,7 @@
 //
 //   fused_rhs     phi, P, u -> u*, P*, phi'   (getTempVari_1/2 + getDtF + getVStar + the phi
 //                 update of getVNew, TTSH3D.cu:537-632, :471-491, :515), all intermediates
-//                 (mu_0, mu_b, the stress S_ab, D_a P_b) kept in shared memory.
+//                 (mu_0, mu_b, the stress S_ab, D_a P_b) kept on chip.
 //   fused_div     u*, P* -> W = div(u*)/dt + i div(P*)/dt   (getStream mode 0, :664-670, with
 //                 the reference's stale halo for neighbours across the periodic boundary)
 //   fused_correct u*, P*, W -> u, P   (getVNew, :505-511)
@@ -12,16 +12,22 @@
 // All three march along z through a tile of TX x TY columns (a "2.5D" sweep): each z-plane of
 // every field the stencils need is staged once in a shared-memory ring of planes, and each
 // thread evaluates the 27-point derivatives / 15-point Laplacians of a 1 x R strip of sites
-// from registers (the strip's 3 x (R+2) x 3 neighbourhood), so warps read shared memory with
-// unit stride. The nested stencils of the RHS (sigma and mu need D P and L P; the velocity
-// update needs D sigma and L mu) are staged: stage 1 forms the products of plane z+1 while
-// the thread of each tile column finishes plane z. It splits those outer stencils into
-// in-plane partial sums and carries the z-combination in registers from plane to plane,
-// so every product plane is read once.
+// from its 3 x (R+2) x 3 neighbourhood, so warps read shared memory with unit stride. The
+// nested stencils of the RHS (sigma and mu need D P and L P; the velocity update needs D sigma
+// and L mu) are staged: stage 1 forms the products of plane z+1 while the thread of each tile
+// column finishes plane z. It splits those outer stencils into in-plane partial sums and
+// carries the z-combination in registers from plane to plane, so every product plane is read
+// once.
 //
-// The stencil arithmetic is the reference's (st_dx/st_dy/st_dz/st_lap of common.cuh) in FP32;
-// the stress enters as one field per component, S_ab = cA phi D_a P_b - zeta phi P_a P_b, whose
-// divergence is the reference's cA * div(sigma) plus the build-defined active stress.
+// fused_rhs keeps its fields in pairs, interleaved in shared memory as float2 ((phi, Px),
+// (Py, Pz), (ux, uy), and pairs of products): one 64-bit load fetches both, and the stencil
+// arithmetic runs on both with the packed FP32 instructions of sm_100+ (add/mul/fma .f32x2, two
+// independent IEEE FP32 operations with round-to-nearest, the same results as two scalar ones).
+//
+// The stencil arithmetic is the reference's 27-point and 15-point weights (st_dx/st_dy/st_dz/
+// st_lap of common.cuh, TTSH3D.cu:3280-3343) in FP32, regrouped separably; the stress enters as
+// one field per component, S_ab = cA phi D_a P_b - zeta phi P_a P_b, whose divergence is the
+// reference's cA * div(sigma) plus the build-defined active stress.
 #include <cstdio>
 #include <stdexcept>
 
@@ -35,26 +41,34 @@ namespace {
 constexpr int TX = 32, TY = 16;   // output tile (columns)
 constexpr int ZC = 64;            // z-planes per block (chunk)
 constexpr int RB = 2;             // strip length (sites per thread) of fused_rhs stage 1
-constexpr int NT = 512;           // threads of fused_rhs: one tile column each in stage 2
+constexpr int NT = 512;           // threads of fused_rhs: one tile column each in phase 2
 constexpr int US = 4;             // strip length of the velocity terms (phase 1)
 
 // fused_rhs regions: A = tile + 2 (phi, P), B = tile + 1 (u, stage-1 products), C = tile.
 constexpr int AW = TX + 4, AH = TY + 4, AN = AW * AH;
 constexpr int BW = TX + 2, BH = TY + 2, BN = BW * BH;
 constexpr int CN = TX * TY;
-// stage-1 products of one plane on B, and the pointwise parts of the update ("partials") on C
-constexpr int QS = 0, QMU = 9, QMU0 = 12, NQ = 13;
-constexpr int PU = 0, PP = 3, PPHI = 6;
-// Shared memory (floats): A ring RA planes x 4 fields; u ring RU x 3; one plane of the 13
-// products; partials ring 2 planes x 7. The A and u rings hold one plane more than the stencils
-// read: the next plane is copied into it (cp.async) while the current ones compute.
+// Products of one plane on B, as float2 pairs (plus one scalar field):
+//   M0 = (mu_0, mu_x), M1 = (mu_y, mu_z)       Laplacians: phi', P*
+//   T0 = (S_xy, S_xz), T1 = (S_yy, S_yz), T2 = (S_zy, S_zz)   divergence columns y, z
+//   T3 = (S_xx, S_yx), and S_zx alone                          divergence column x
+constexpr int PM0 = 0, PM1 = 1, PT0 = 2, PT1 = 3, PT2 = 4, PT3 = 5, NPR = 6;
+// Pointwise parts of the update on C ("partials"), float2 pairs:
+//   Q0 = (u_x, u_y) terms, Q1 = (u_z term, phi term), Q2 = (P_x, P_y) terms, Q3 = (P_z term, -)
+constexpr int NPQ = 4;
+// Shared memory (bytes): A ring RA planes x 2 pairs; u ring RU planes x ((ux, uy) pair + uz);
+// one plane of products; partials ring 2 planes. The A and u rings hold one plane more than the
+// stencils read: the next plane is copied into it (cp.async) while the current ones compute.
 constexpr int RA = 4, RU = 4;
-constexpr int SA_OFF = 0;
-constexpr int SU_OFF = SA_OFF + RA * 4 * AN;
-constexpr int SB_OFF = SU_OFF + RU * 3 * BN;
-constexpr int SQ_OFF = SB_OFF + NQ * BN;
-constexpr int RHS_SMEM_FLOATS = SQ_OFF + 2 * 7 * CN;
-constexpr size_t RHS_SMEM = RHS_SMEM_FLOATS * sizeof(float);
+constexpr size_t OFF_A = 0;
+constexpr size_t OFF_U01 = OFF_A + (size_t)RA * 2 * AN * sizeof(float2);
+constexpr size_t OFF_U2 = OFF_U01 + (size_t)RU * BN * sizeof(float2);
+constexpr size_t OFF_PR = OFF_U2 + (size_t)RU * BN * sizeof(float);
+constexpr size_t OFF_SZX = OFF_PR + (size_t)NPR * BN * sizeof(float2);
+constexpr size_t OFF_PQ = OFF_SZX + (size_t)BN * sizeof(float);
+constexpr size_t RHS_SMEM = OFF_PQ + (size_t)2 * NPQ * CN * sizeof(float2);
+static_assert(OFF_U01 % 16 == 0 && OFF_U2 % 16 == 0 && OFF_PR % 16 == 0 && OFF_SZX % 16 == 0 && OFF_PQ % 16 == 0,
+              "16-byte aligned regions");
 // phase-1 thread roles of fused_rhs: stage-1 strips of the B region, then the velocity strips
 constexpr int NS1 = (BW * BH) / RB;                   // 306 stage-1 strips
 constexpr int NU0 = ((NS1 + 31) / 32) * 32;           // first velocity thread (warp aligned)
@@ -69,107 +83,112 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
 }
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
-}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-// A 3 (planes) x (R+2) (rows) x 3 (columns) neighbourhood held in registers, for a strip of R
-// sites stacked in y. F(dx,dy,dz) of site k reads v[1+dz][1+k+dy][1+dx].
-template <int R>
-struct Hood {
-  float v[3][R + 2][3];
-  __device__ __forceinline__ void load(const float* p0, const float* p1, const float* p2, int W, int x, int y0) {
-    const float* pl[3] = {p0, p1, p2};
-#pragma unroll
-    for (int z = 0; z < 3; ++z)
-#pragma unroll
-      for (int r = 0; r < R + 2; ++r)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) v[z][r][c] = pl[z][(y0 - 1 + r) * W + (x - 1 + c)];
-  }
-};
-template <int R>
-struct HoodAcc {
-  const Hood<R>* h;
-  int k;
-  __device__ __forceinline__ float operator()(int dx, int dy, int dz) const { return h->v[1 + dz][1 + k + dy][1 + dx]; }
-};
+// Arithmetic on one value (float) or a pair (float2, packed FP32).
+__device__ __forceinline__ float vadd(float a, float b) { return a + b; }
+__device__ __forceinline__ float vsub(float a, float b) { return a - b; }
+__device__ __forceinline__ float vmul(float a, float b) { return a * b; }
+__device__ __forceinline__ float vfma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ float vsplat(float a, float) { return a; }
+__device__ __forceinline__ float2 vadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 vsub(float2 a, float2 b) {
+  float2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;"
+      : "=l"(*reinterpret_cast<unsigned long long*>(&d))
+      : "l"(*reinterpret_cast<const unsigned long long*>(&a)), "l"(*reinterpret_cast<const unsigned long long*>(&b)));
+  return d;
+}
+__device__ __forceinline__ float2 vmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 vfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 vsplat(float a, float2) { return make_float2(a, a); }
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
-// Separable evaluation on a Hood (FP32 form). With s = [1, 4, 1] and delta = [-1, 0, 1]:
+// Separable evaluation (FP32). With s = [1, 4, 1] and delta = [-1, 0, 1]:
 //   D_x = c2h/36 * delta_x s_y s_z,  D_y = c2h/36 * s_x delta_y s_z,  D_z = c2h/36 * s_x s_y delta_z,
 //   L = cl12 * (8 corners) + cl23 * (6 faces) - cl143 * centre  (corners = c_x c_y c_z, c = [1, 0, 1]),
-// the reference's 27-point and 15-point weights (TTSH3D.cu:3280-3343) regrouped so that the
-// z-combinations of each (row, column) are shared by the R sites of the strip.
+// the reference's 27-point and 15-point weights (TTSH3D.cu:3280-3343) regrouped. Each row of the
+// neighbourhood (3 planes x 3 columns) is reduced to the few sums the R sites of the strip share.
 struct SepK {
   float d;  // c2h / 36
   float l12, l23, l143;
 };
-template <int R, bool DX, bool DY, bool DZ, bool LAP>
-__device__ __forceinline__ void sep_eval(const Hood<R>& h, const SepK& k, float* dx, float* dy, float* dz, float* lap) {
-  float cz[R + 2][3], sz[R + 2][3], dzr[R + 2][3];
+// ld(z, r, c): the value at plane z (0..2 = offset -1..1), strip row r (0..R+1 = offset -1..R),
+// column c (0..2 = offset -1..1). ctr[i] receives the centre value of site i.
+template <int R, bool DX, bool DY, bool DZ, bool LAP, class V, class LD>
+__device__ __forceinline__ void sep_rows(const LD& ld, const SepK& k, V* dx, V* dy, V* dz, V* lap, V* ctr) {
+  const V four = vsplat(4.f, V()), kd = vsplat(k.d, V());
+  V a[R + 2], b[R + 2], c[R + 2], e[R + 2], f[R + 2], g[R + 2], h[R + 2];
 #pragma unroll
-  for (int r = 0; r < R + 2; ++r)
+  for (int r = 0; r < R + 2; ++r) {
+    V v0[3], v1[3], v2[3], cz[3], sz[3], dzr[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      cz[r][c] = h.v[0][r][c] + h.v[2][r][c];
-      sz[r][c] = fmaf(4.f, h.v[1][r][c], cz[r][c]);
-      dzr[r][c] = h.v[2][r][c] - h.v[0][r][c];
+    for (int q = 0; q < 3; ++q) {
+      v0[q] = ld(0, r, q);
+      v1[q] = ld(1, r, q);
+      v2[q] = ld(2, r, q);
+      cz[q] = vadd(v0[q], v2[q]);
+      sz[q] = vfma(four, v1[q], cz[q]);
+      dzr[q] = vsub(v2[q], v0[q]);
     }
+    a[r] = vsub(sz[2], sz[0]);                       // delta_x of s_z
+    b[r] = vfma(four, sz[1], vadd(sz[0], sz[2]));    // s_x of s_z
+    c[r] = vfma(four, dzr[1], vadd(dzr[0], dzr[2])); // s_x of delta_z
+    e[r] = vadd(cz[0], cz[2]);                       // corners of the row
+    f[r] = cz[1];                                    // z faces
+    g[r] = vadd(v1[0], v1[2]);                       // x faces
+    h[r] = v1[1];                                    // centre column of the centre plane
+  }
 #pragma unroll
   for (int i = 0; i < R; ++i) {
-    if (DX) {
-      const float a = fmaf(4.f, sz[i + 1][2], sz[i][2] + sz[i + 2][2]);
-      const float b = fmaf(4.f, sz[i + 1][0], sz[i][0] + sz[i + 2][0]);
-      dx[i] = k.d * (a - b);
-    }
-    if (DY) {
-      const float e0 = sz[i + 2][0] - sz[i][0], e1 = sz[i + 2][1] - sz[i][1], e2 = sz[i + 2][2] - sz[i][2];
-      dy[i] = k.d * fmaf(4.f, e1, e0 + e2);
-    }
-    if (DZ) {
-      const float f0 = fmaf(4.f, dzr[i + 1][0], dzr[i][0] + dzr[i + 2][0]);
-      const float f1 = fmaf(4.f, dzr[i + 1][1], dzr[i][1] + dzr[i + 2][1]);
-      const float f2 = fmaf(4.f, dzr[i + 1][2], dzr[i][2] + dzr[i + 2][2]);
-      dz[i] = k.d * fmaf(4.f, f1, f0 + f2);
-    }
+    if (DX) dx[i] = vmul(kd, vfma(four, a[i + 1], vadd(a[i], a[i + 2])));
+    if (DY) dy[i] = vmul(kd, vsub(b[i + 2], b[i]));
+    if (DZ) dz[i] = vmul(kd, vfma(four, c[i + 1], vadd(c[i], c[i + 2])));
     if (LAP) {
-      const float corners = (cz[i][0] + cz[i][2]) + (cz[i + 2][0] + cz[i + 2][2]);
-      const float faces = (cz[i + 1][1] + h.v[1][i + 1][0]) + (h.v[1][i + 1][2] + h.v[1][i][1]) + h.v[1][i + 2][1];
-      lap[i] = fmaf(k.l12, corners, fmaf(k.l23, faces, -k.l143 * h.v[1][i + 1][1]));
+      const V corners = vadd(e[i], e[i + 2]);
+      const V faces = vadd(vadd(f[i + 1], g[i + 1]), vadd(h[i], h[i + 2]));
+      lap[i] = vfma(vsplat(k.l12, V()), corners,
+                    vfma(vsplat(k.l23, V()), faces, vmul(vsplat(-k.l143, V()), h[i + 1])));
     }
+    if (ctr) ctr[i] = h[i + 1];
   }
 }
 
-// Interleaved-complex variant (one component of a float2 plane).
-template <int R>
-struct Hood2 {
-  float2 v[3][R + 2][3];
-  __device__ __forceinline__ void load(const float2* p0, const float2* p1, const float2* p2, int W, int x, int y0) {
-    const float2* pl[3] = {p0, p1, p2};
-#pragma unroll
-    for (int z = 0; z < 3; ++z)
-#pragma unroll
-      for (int r = 0; r < R + 2; ++r)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) v[z][r][c] = pl[z][(y0 - 1 + r) * W + (x - 1 + c)];
-  }
-};
-template <int R, int COMP>
-struct Hood2Acc {
-  const Hood2<R>* h;
-  int k;
-  __device__ __forceinline__ float operator()(int dx, int dy, int dz) const {
-    const float2 t = h->v[1 + dz][1 + k + dy][1 + dx];
-    return COMP == 0 ? t.x : t.y;
-  }
-};
+// Plane partial sums of the outer stencils over a product plane, at one column (F points at it):
+//   Laplacian: an off-centre plane adds G = l12 (its 4 diagonal sites) + l23 (its centre site),
+//   the centre plane adds H = l23 (its 4 edge sites) - l143 (its centre site);
+//   divergence: X = delta_x s_y, Y = s_x delta_y (weight s_z over the planes), Z = s_x s_y
+//   (weight delta_z).
+template <class V>
+__device__ __forceinline__ void lap_part(const V* F, int W, const SepK& k, V& G, V& H) {
+  const V v11 = F[0];
+  const V dg = vadd(vadd(F[-W - 1], F[-W + 1]), vadd(F[W - 1], F[W + 1]));
+  const V ed = vadd(vadd(F[-W], F[W]), vadd(F[-1], F[1]));
+  G = vfma(vsplat(k.l12, V()), dg, vmul(vsplat(k.l23, V()), v11));
+  H = vfma(vsplat(k.l23, V()), ed, vmul(vsplat(-k.l143, V()), v11));
+}
+template <class V>
+__device__ __forceinline__ V x_part(const V* X, int W) {
+  const V four = vsplat(4.f, V());
+  return vsub(vfma(four, X[1], vadd(X[-W + 1], X[W + 1])), vfma(four, X[-1], vadd(X[-W - 1], X[W - 1])));
+}
+template <class V>
+__device__ __forceinline__ V y_part(const V* Y, int W) {
+  return vfma(vsplat(4.f, V()), vsub(Y[W], Y[-W]), vadd(vsub(Y[W - 1], Y[-W - 1]), vsub(Y[W + 1], Y[-W + 1])));
+}
+template <class V>
+__device__ __forceinline__ V z_part(const V* Z, int W) {
+  const V four = vsplat(4.f, V());
+  const V t0 = vfma(four, Z[-1], vadd(Z[-W - 1], Z[W - 1]));
+  const V t1 = vfma(four, Z[0], vadd(Z[-W], Z[W]));
+  const V t2 = vfma(four, Z[1], vadd(Z[-W + 1], Z[W + 1]));
+  return vfma(four, t1, vadd(t0, t2));
+}
 
 // ------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __restrict__ insts, int par, int nchunk) {
-  extern __shared__ __align__(16) float sm[];
+  extern __shared__ __align__(16) unsigned char smr[];
   const int N = insts[0].N;
   const InstDev<float>& I = insts[blockIdx.z / nchunk];
   const Phys<float> p = I.ph;  // by value: read once, kept in registers
@@ -185,10 +204,12 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
   float* const oPs[3] = {I.Ps[par ^ 1][0], I.Ps[par ^ 1][1], I.Ps[par ^ 1][2]};
   float* const ophi = I.phi[par ^ 1];
   float* const phic = I.phic;
-  float* sA = sm + SA_OFF;  // [RA][4][AN]: phi, Px, Py, Pz
-  float* sU = sm + SU_OFF;  // [RU][3][BN]
-  float* sB = sm + SB_OFF;  // [NQ][BN]: products of plane b
-  float* sQ = sm + SQ_OFF;  // [2][7][CN]
+  float2* const sA = reinterpret_cast<float2*>(smr + OFF_A);      // [RA][2][AN]: (phi, Px), (Py, Pz)
+  float2* const sU01 = reinterpret_cast<float2*>(smr + OFF_U01);  // [RU][BN]: (ux, uy)
+  float* const sU2 = reinterpret_cast<float*>(smr + OFF_U2);      // [RU][BN]: uz
+  float2* const sPr = reinterpret_cast<float2*>(smr + OFF_PR);    // [NPR][BN]
+  float* const sSzx = reinterpret_cast<float*>(smr + OFF_SZX);    // [BN]
+  float2* const sQ = reinterpret_cast<float2*>(smr + OFF_PQ);     // [2][NPQ][CN]
   const int tid = threadIdx.x;
   const int niter = (z1 - z0) + 4;
 
@@ -197,23 +218,24 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
   // c = a - 2; issue(i + 1) runs during iteration i.
   auto issue = [&](int i) {
     const int za = ((z0 - 2 + i) % N + N) % N;
-    float* dst = sA + (i % RA) * 4 * AN;
+    float* dst = reinterpret_cast<float*>(sA + (i % RA) * 2 * AN);
     for (int t = tid; t < AN; t += NT) {
       const int ay = t / AW, ax = t - ay * AW;
       const size_t g = (size_t)za * NN + (size_t)wrapN(y0 - 2 + ay, N) * N + wrapN(x0 - 2 + ax, N);
-      cp_async4(dst + t, gphi + g);
-      cp_async4(dst + AN + t, gP[0] + g);
-      cp_async4(dst + 2 * AN + t, gP[1] + g);
-      cp_async4(dst + 3 * AN + t, gP[2] + g);
+      cp_async4(dst + 2 * t, gphi + g);
+      cp_async4(dst + 2 * t + 1, gP[0] + g);
+      cp_async4(dst + 2 * (AN + t), gP[1] + g);
+      cp_async4(dst + 2 * (AN + t) + 1, gP[2] + g);
     }
     const int zu = ((z0 - 3 + i) % N + N) % N;
-    float* du = sU + (i % RU) * 3 * BN;
+    float* du = reinterpret_cast<float*>(sU01 + (i % RU) * BN);
+    float* dz = sU2 + (i % RU) * BN;
     for (int t = tid; t < BN; t += NT) {
       const int by = t / BW, bx = t - by * BW;
       const size_t g = (size_t)zu * NN + (size_t)wrapN(y0 - 1 + by, N) * N + wrapN(x0 - 1 + bx, N);
-      cp_async4(du + t, gU[0] + g);
-      cp_async4(du + BN + t, gU[1] + g);
-      cp_async4(du + 2 * BN + t, gU[2] + g);
+      cp_async4(du + 2 * t, gU[0] + g);
+      cp_async4(du + 2 * t + 1, gU[1] + g);
+      cp_async4(dz + t, gU[2] + g);
     }
     cp_async_commit();
   };
@@ -221,11 +243,12 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
   const int qx = tid % TX, qy = tid / TX;
   const size_t gc = (size_t)(y0 + qy) * N + (x0 + qx);
   const int qo = (qy + 1) * BW + (qx + 1);  // its B-region index
-  // z-combinations carried from plane to plane (phase 2): for the Laplacians of mu_b, mu_0,
-  // rL1 = the partial sum of the plane just finished + 1, rL2 = that of the plane after it;
-  // likewise rD1 / rD2 for the stress divergence of column b
-  float rL1[4] = {0.f, 0.f, 0.f, 0.f}, rL2[4] = {0.f, 0.f, 0.f, 0.f};
-  float rD1[3] = {0.f, 0.f, 0.f}, rD2[3] = {0.f, 0.f, 0.f};
+  // z-combinations carried from plane to plane (phase 2): for the Laplacians of (mu_0, mu_x),
+  // (mu_y, mu_z), rL1 = the partial sum of the plane just finished + 1, rL2 = that of the plane
+  // after it; likewise rD1 / rD2 for the stress divergence of columns (y, z) and x
+  float2 rL1[2] = {f2(0.f, 0.f), f2(0.f, 0.f)}, rL2[2] = {f2(0.f, 0.f), f2(0.f, 0.f)};
+  float2 rD1 = f2(0.f, 0.f), rD2 = f2(0.f, 0.f);
+  float rX1 = 0.f, rX2 = 0.f;
   issue(0);
   for (int i = 0; i < niter; ++i) {
     cp_async_wait_all();
@@ -237,12 +260,9 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
     // ---- phase 1a, stage 1 at plane b = z0 - 3 + i over B (tile+1): the products mu_0, mu_b,
     //      S_ab that phase 2 differentiates, and on the tile the pointwise parts of the update
     if (i >= 2 && tid < NS1) {
-      const float* a0 = sA + ((i + RA - 2) % RA) * 4 * AN;  // plane b-1
-      const float* a1 = sA + ((i + RA - 1) % RA) * 4 * AN;  // plane b
-      const float* a2 = sA + (i % RA) * 4 * AN;             // plane b+1
-      const float* ub = sU + (i % RU) * 3 * BN;             // u at plane b
-      float* bq = sB;
-      float* pq = sQ + (i & 1) * 7 * CN;
+      const float2* a0 = sA + ((i + RA - 2) % RA) * 2 * AN;  // plane b-1
+      const float2* a1 = sA + ((i + RA - 1) % RA) * 2 * AN;  // plane b
+      const float2* a2 = sA + (i % RA) * 2 * AN;             // plane b+1
       // strips of the B region: warps take 32 consecutive columns of one strip row (unit-stride
       // shared-memory access); the last BW - 32 columns of every row come after them
       constexpr int NSR = BH / RB, NMAIN = 32 * NSR;
@@ -250,64 +270,74 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
       int bx, by0;
       if (s < NMAIN) { bx = s & 31; by0 = (s >> 5) * RB; }
       else { const int e = s - NMAIN; bx = 32 + e % (BW - 32); by0 = (e / (BW - 32)) * RB; }
-      const int ax = bx + 1, ay0 = by0 + 1;  // A coordinates
-      float phc[RB], lphi[RB], dphi[3][RB];
+      const int base = by0 * AW + bx;  // A index of row offset -1, column offset -1 of site 0
+      // pair 0 = (phi, Px), pair 1 = (Py, Pz): D_a (3), L and the centre value of each site
+      float2 D0[3][RB], L0[RB], C0[RB], D1[3][RB], L1[RB], C1[RB];
       {
-        Hood<RB> h;
-        h.load(a0, a1, a2, AW, ax, ay0);
-#pragma unroll
-        for (int k = 0; k < RB; ++k) phc[k] = h.v[1][1 + k][1];
-        sep_eval<RB, true, true, true, true>(h, sk, dphi[0], dphi[1], dphi[2], lphi);
+        auto ld = [&](int z, int r, int c) {
+          const float2* pl = z == 0 ? a0 : (z == 1 ? a1 : a2);
+          return pl[base + r * AW + c];
+        };
+        sep_rows<RB, true, true, true, true, float2>(ld, sk, D0[0], D0[1], D0[2], L0, C0);
       }
-      float Pc[3][RB], DP[3][3][RB];  // DP[a][b] = D_a P_b
-#pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        Hood<RB> h;
-        h.load(a0 + (1 + b) * AN, a1 + (1 + b) * AN, a2 + (1 + b) * AN, AW, ax, ay0);
-        float lp[RB];
-        sep_eval<RB, true, true, true, true>(h, sk, DP[0][b], DP[1][b], DP[2][b], lp);
-#pragma unroll
-        for (int k = 0; k < RB; ++k) {
-          Pc[b][k] = h.v[1][1 + k][1];
-          bq[(QMU + b) * BN + (by0 + k) * BW + bx] = fmaf(p.La2, lp[k], phc[k] * Pc[b][k]);  // mu_b (:571-573)
-        }
+      {
+        auto ld = [&](int z, int r, int c) {
+          const float2* pl = z == 0 ? a0 : (z == 1 ? a1 : a2);
+          return pl[AN + base + r * AW + c];
+        };
+        sep_rows<RB, true, true, true, true, float2>(ld, sk, D1[0], D1[1], D1[2], L1, C1);
       }
+      const float2* ubp = sU01 + (i % RU) * BN;  // u at plane b
+      const float* ubz = sU2 + (i % RU) * BN;
+      float2* pq = sQ + (i & 1) * NPQ * CN;
 #pragma unroll
       for (int k = 0; k < RB; ++k) {
-        const float ph = phc[k];
         const int o = (by0 + k) * BW + bx;
-        const float mu0 = p.aPhi2 * (ph - 3 * ph * ph + 2 * ph * ph * ph) - p.kPhi * lphi[k];  // mu_0 (:567)
-        bq[QMU0 * BN + o] = mu0;
+        const float ph = C0[k].x, px = C0[k].y, py = C1[k].x, pz = C1[k].y;
+        // mu_0 = aPhi 2(phi - 3phi^2 + 2phi^3) - kPhi L phi (:567), mu_b = phi P_b + La^2 L P_b (:571-573)
+        const float poly = p.aPhi2 * (ph - 3 * ph * ph + 2 * ph * ph * ph);
+        const float2 M0 = vfma(f2(-p.kPhi, p.La2), L0[k], f2(poly, ph * px));
+        const float2 M1 = vfma(vsplat(p.La2, float2()), L1[k], vmul(vsplat(ph, float2()), C1[k]));
+        sPr[PM0 * BN + o] = M0;
+        sPr[PM1 * BN + o] = M1;
+        // S_ab = cA phi D_a P_b - zeta phi P_a P_b (:587-595 and the active stress)
+        const float cph = p.cA * ph, zph = p.zeta * ph;
+        const float Pa[3] = {px, py, pz};
+        float sx[3];
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-          for (int b = 0; b < 3; ++b) {
-            float sv = p.cA * (ph * DP[a][b][k]);  // cA * sigma_ab (:587-595)
-            if (p.zeta != 0.f) sv -= p.zeta * (ph * Pc[a][k] * Pc[b][k]);
-            bq[(QS + a * 3 + b) * BN + o] = sv;
-          }
+        for (int a = 0; a < 3; ++a) {
+          sPr[(PT0 + a) * BN + o] = vfma(vsplat(cph, float2()), D1[a][k], vmul(vsplat(-zph * Pa[a], float2()), C1[k]));
+          sx[a] = fmaf(cph, D0[a][k].y, -zph * Pa[a] * px);
+        }
+        sPr[PT3 * BN + o] = f2(sx[0], sx[1]);
+        sSzx[o] = sx[2];
         const int cx = bx - 1, cy = by0 + k - 1;
         if (cx >= 0 && cx < TX && cy >= 0 && cy < TY) {
-          // pointwise parts of getDtF (:617-631) at this site of plane b
+          // pointwise parts of getDtF (:617-631) at this site of plane b:
+          //   u_b:  mu_0 D_b phi;  phi: -u.D phi;
+          //   P_b:  -(u + lambda0 P).D P_b - P_b (alpha phi + beta |P|^2 + A |D phi|^2 |P|^2)
+          //         - A |P| (D phi . P) D_b phi
           const int c = cy * TX + cx;
-          const float vx = ub[o], vy = ub[BN + o], vz = ub[2 * BN + o];
-          const float px = Pc[0][k], py = Pc[1][k], pz = Pc[2][k];
+          const float2 uxy = ubp[o];
+          const float vx = uxy.x, vy = uxy.y, vz = ubz[o];
+          const float mu0 = M0.x;
+          const float gx = D0[0][k].x, gy = D0[1][k].x, gz = D0[2][k].x;  // D phi
           const float P2 = px * px + py * py + pz * pz;
-          const float dPhi2 = dphi[0][k] * dphi[0][k] + dphi[1][k] * dphi[1][k] + dphi[2][k] * dphi[2][k];
-#pragma unroll
-          for (int b = 0; b < 3; ++b) {
-            pq[(PU + b) * CN + c] = mu0 * dphi[b][k];  // mu_0 D_b phi
-            const float pb = Pc[b][k];
-            float cub;
-            if (b == 0) cub = px * px * px + px * py * py + px * pz * pz;
-            else if (b == 1) cub = px * py * px + py * py * py + py * pz * pz;
-            else cub = px * pz * px + py * pz * py + pz * pz * pz;
-            const float Ab = dphi[0][k] * dphi[b][k] * px + dphi[1][k] * dphi[b][k] * py + dphi[2][k] * dphi[b][k] * pz;
-            pq[(PP + b) * CN + c] = -vx * DP[0][b][k] - vy * DP[1][b][k] - vz * DP[2][b][k] - p.alpha * ph * pb -
-                                    p.beta * P2 * pb - p.lambda0 * (px * DP[0][b][k] + py * DP[1][b][k] + pz * DP[2][b][k]) -
-                                    p.A * (dPhi2 * cub + sqrtf(P2) * Ab);
-          }
-          pq[PPHI * CN + c] = -vx * dphi[0][k] - vy * dphi[1][k] - vz * dphi[2][k];
+          const float G2 = gx * gx + gy * gy + gz * gz;
+          const float GP = gx * px + gy * py + gz * pz;
+          const float kap = p.alpha * ph + P2 * (p.beta + p.A * G2);
+          const float m = p.A * sqrtf(P2) * GP;
+          const float wx = fmaf(p.lambda0, px, vx), wy = fmaf(p.lambda0, py, vy), wz = fmaf(p.lambda0, pz, vz);
+          pq[0 * CN + c] = f2(mu0 * gx, mu0 * gy);
+          pq[1 * CN + c] = f2(mu0 * gz, -(vx * gx + vy * gy + vz * gz));
+          const float ppx = -(wx * D0[0][k].y + wy * D0[1][k].y + wz * D0[2][k].y) - kap * px - m * gx;
+          float2 t = vmul(vsplat(wx, float2()), D1[0][k]);
+          t = vfma(vsplat(wy, float2()), D1[1][k], t);
+          t = vfma(vsplat(wz, float2()), D1[2][k], t);
+          t = vfma(vsplat(kap, float2()), C1[k], t);
+          t = vfma(vsplat(m, float2()), f2(gy, gz), t);
+          pq[2 * CN + c] = f2(ppx, -t.x);
+          pq[3 * CN + c] = f2(-t.y, 0.f);
         }
       }
     }
@@ -317,88 +347,97 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
     if (i >= 4 && tid >= NU0 && tid < NU0 + NUS) {
       const int s = tid - NU0;
       const int vx = s & 31, vy0 = (s >> 5) * US;  // tile coordinates of the strip
-      const float* u0 = sU + ((i + RU - 2) % RU) * 3 * BN;  // plane c-1
-      const float* u1 = sU + ((i + RU - 1) % RU) * 3 * BN;  // plane c
-      const float* u2 = sU + (i % RU) * 3 * BN;             // plane c+1
-      float* pq = sQ + ((i + 1) & 1) * 7 * CN;
-      float uc[3][US];
+      const int sl0 = (i + RU - 2) % RU, sl1 = (i + RU - 1) % RU, sl2 = i % RU;  // planes c-1, c, c+1
+      const int base = vy0 * BW + vx;  // B index of row offset -1, column offset -1 of site 0
+      float2 Dp[3][US], Lp[US], Cp[US];
+      float Dz[3][US], Lz[US], Cz[US];
+      {
+        auto ld = [&](int z, int r, int c) {
+          const int sl = z == 0 ? sl0 : (z == 1 ? sl1 : sl2);
+          return sU01[sl * BN + base + r * BW + c];
+        };
+        sep_rows<US, true, true, true, true, float2>(ld, sk, Dp[0], Dp[1], Dp[2], Lp, Cp);
+      }
+      {
+        auto ld = [&](int z, int r, int c) {
+          const int sl = z == 0 ? sl0 : (z == 1 ? sl1 : sl2);
+          return sU2[sl * BN + base + r * BW + c];
+        };
+        sep_rows<US, true, true, true, true, float>(ld, sk, Dz[0], Dz[1], Dz[2], Lz, Cz);
+      }
+      float2* pq = sQ + ((i + 1) & 1) * NPQ * CN;
 #pragma unroll
-      for (int b = 0; b < 3; ++b)
-#pragma unroll
-        for (int k = 0; k < US; ++k) uc[b][k] = u1[b * BN + (vy0 + 1 + k) * BW + vx + 1];
-#pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        float dx[US], dy[US], dz[US], lu[US];
-        {
-          Hood<US> h;
-          h.load(u0 + b * BN, u1 + b * BN, u2 + b * BN, BW, vx + 1, vy0 + 1);
-          sep_eval<US, true, true, true, true>(h, sk, dx, dy, dz, lu);
-        }
-#pragma unroll
-        for (int k = 0; k < US; ++k)
-          pq[(PU + b) * CN + (vy0 + k) * TX + vx] +=
-              -uc[0][k] * dx[k] - uc[1][k] * dy[k] - uc[2][k] * dz[k] + p.mu * lu[k];
+      for (int k = 0; k < US; ++k) {
+        const int c = (vy0 + k) * TX + vx;
+        const float ux = Cp[k].x, uy = Cp[k].y, uz = Cz[k];
+        float2 t = vmul(vsplat(-ux, float2()), Dp[0][k]);
+        t = vfma(vsplat(-uy, float2()), Dp[1][k], t);
+        t = vfma(vsplat(-uz, float2()), Dp[2][k], t);
+        t = vfma(vsplat(p.mu, float2()), Lp[k], t);
+        const float tz = fmaf(p.mu, Lz[k], -(ux * Dz[0][k] + uy * Dz[1][k] + uz * Dz[2][k]));
+        pq[0 * CN + c] = vadd(pq[0 * CN + c], t);
+        pq[1 * CN + c].x += tz;
       }
     }
     __syncthreads();
     // ---- phase 2, one tile column per thread: the in-plane partial sums of the outer stencils
     //      over the products of plane b, carried in z; plane c = b - 1 is then complete
     if (i >= 2) {
-      const float* bq = sB + qo;
-      // 15-point Laplacian L = l12 (8 corners) + l23 (6 faces) - l143 (centre) (:3328-3343):
-      // an off-centre plane p adds G_p = l12 (its 4 diagonal sites) + l23 (its centre site),
-      // the centre plane adds H_p = l23 (its 4 edge sites) - l143 (its centre site)
-      float lmu[4];
+      float2 lm[2];
 #pragma unroll
-      for (int f = 0; f < 4; ++f) {
-        const float* F = bq + (QMU + f) * BN;
-        const float v11 = F[0];
-        const float dg = (F[-BW - 1] + F[-BW + 1]) + (F[BW - 1] + F[BW + 1]);
-        const float ed = (F[-BW] + F[BW]) + (F[-1] + F[1]);
-        const float G = fmaf(sk.l12, dg, sk.l23 * v11);
-        const float H = fmaf(sk.l23, ed, -sk.l143 * v11);
-        lmu[f] = rL1[f] + G;
-        rL1[f] = rL2[f] + H;
-        rL2[f] = G;
+      for (int q = 0; q < 2; ++q) {
+        float2 G, H;
+        lap_part(sPr + (PM0 + q) * BN + qo, BW, sk, G, H);
+        lm[q] = vadd(rL1[q], G);
+        rL1[q] = vadd(rL2[q], H);
+        rL2[q] = G;
       }
-      // divergence of stress column b, d/36 (delta_x s_y s_z S_xb + s_x delta_y s_z S_yb +
-      // s_x s_y delta_z S_zb): the plane adds Q = delta_x s_y S_xb + s_x delta_y S_yb with weight
-      // s_z = (1, 4, 1) and Z = s_x s_y S_zb with weight delta_z = (-1, 0, 1) over planes c-1, c, c+1
-      float dv[3];
-#pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        const float* X = bq + (QS + 0 * 3 + b) * BN;
-        const float* Y = bq + (QS + 1 * 3 + b) * BN;
-        const float* Z = bq + (QS + 2 * 3 + b) * BN;
-        const float xr = fmaf(4.f, X[1], X[-BW + 1] + X[BW + 1]) - fmaf(4.f, X[-1], X[-BW - 1] + X[BW - 1]);
-        const float yr = fmaf(4.f, Y[BW] - Y[-BW], (Y[BW - 1] - Y[-BW - 1]) + (Y[BW + 1] - Y[-BW + 1]));
-        const float t0 = fmaf(4.f, Z[-1], Z[-BW - 1] + Z[BW - 1]);
-        const float t1 = fmaf(4.f, Z[0], Z[-BW] + Z[BW]);
-        const float t2 = fmaf(4.f, Z[1], Z[-BW + 1] + Z[BW + 1]);
-        const float zr = fmaf(4.f, t1, t0 + t2);
-        const float Q = xr + yr;
-        dv[b] = sk.d * (rD1[b] + Q + zr);
-        rD1[b] = fmaf(4.f, Q, rD2[b]);
-        rD2[b] = Q - zr;
+      // divergence columns (y, z): X of T0, Y of T1, Z of T2 (packed)
+      const float2 Q = vadd(x_part(sPr + PT0 * BN + qo, BW), y_part(sPr + PT1 * BN + qo, BW));
+      const float2 Zr = z_part(sPr + PT2 * BN + qo, BW);
+      const float2 dvyz = vadd(vadd(rD1, Q), Zr);
+      rD1 = vfma(vsplat(4.f, float2()), Q, rD2);
+      rD2 = vsub(Q, Zr);
+      // divergence column x: X of S_xx (T3.x), Y of S_yx (T3.y), Z of S_zx
+      float dvx;
+      {
+        const float2* T = sPr + PT3 * BN + qo;
+        const float2 tmm = T[-BW - 1], tm0 = T[-BW], tmp = T[-BW + 1], t0m = T[-1], t0p = T[1];
+        const float2 tpm = T[BW - 1], tp0 = T[BW], tpp = T[BW + 1];
+        const float xr = fmaf(4.f, t0p.x, tmp.x + tpp.x) - fmaf(4.f, t0m.x, tmm.x + tpm.x);
+        const float yr = fmaf(4.f, tp0.y - tm0.y, (tpm.y - tmm.y) + (tpp.y - tmp.y));
+        const float zr = z_part(sSzx + qo, BW);
+        const float Qx = xr + yr;
+        dvx = rX1 + Qx + zr;
+        rX1 = fmaf(4.f, Qx, rX2);
+        rX2 = Qx - zr;
       }
       if (i >= 4) {
         const int zc = z0 - 4 + i;
-        const float* pq = sQ + ((i + 1) & 1) * 7 * CN;        // plane c, stage 1 + velocity terms
-        const float* uc = sU + ((i + RU - 1) % RU) * 3 * BN;  // u at plane c
-        const float* ac = sA + ((i + RA - 2) % RA) * 4 * AN;  // phi, P at plane c
+        const float2* pq = sQ + ((i + 1) & 1) * NPQ * CN;  // plane c: stage 1 + velocity terms
+        const int sl = (i + RU - 1) % RU;                  // u at plane c
+        const float2* ac = sA + ((i + RA - 2) % RA) * 2 * AN;  // phi, P at plane c
         const int c = qy * TX + qx, oa = (qy + 2) * AW + (qx + 2);
         const size_t g = (size_t)zc * NN + gc;
+        const float2 q0 = pq[0 * CN + c], q1 = pq[1 * CN + c], q2 = pq[2 * CN + c], q3 = pq[3 * CN + c];
+        const float2 uxy = sU01[sl * BN + qo];
+        const float uz = sU2[sl * BN + qo];
+        const float2 A0 = ac[oa], A1 = ac[AN + oa];
         // u*_b = u_b + dt d/dt u_b (:480-482)
-#pragma unroll
-        for (int b = 0; b < 3; ++b) oUs[b][g] = uc[b * BN + qo] + p.dt * (pq[(PU + b) * CN + c] + dv[b]);
+        oUs[0][g] = fmaf(p.dt, fmaf(sk.d, dvx, q0.x), uxy.x);
+        const float2 us = vfma(vsplat(p.dt, float2()), vfma(vsplat(sk.d, float2()), dvyz, f2(q0.y, q1.x)), f2(uxy.y, uz));
+        oUs[1][g] = us.x;
+        oUs[2][g] = us.y;
         // P*_b = P_b + dt (pointwise part + eta L mu_b) (:623-629, :486-488)
-#pragma unroll
-        for (int b = 0; b < 3; ++b) oPs[b][g] = ac[(1 + b) * AN + oa] + p.dt * (pq[(PP + b) * CN + c] + p.eta * lmu[b]);
+        oPs[0][g] = fmaf(p.dt, fmaf(p.eta, lm[0].y, q2.x), A0.y);
+        const float2 ps = vfma(vsplat(p.dt, float2()), vfma(vsplat(p.eta, float2()), lm[1], f2(q2.y, q3.x)), A1);
+        oPs[1][g] = ps.x;
+        oPs[2][g] = ps.y;
         // phi' = phi + dt (-u.D phi + gamma L mu_0) (:631, :515), compensated: the part of the
         // increment that rounding drops from phi is carried to the next step (otherwise
         // increments below half an ulp of phi are lost, a systematic mass drift)
-        const float ph = ac[oa];
-        const float inc = fmaf(p.dt, pq[PPHI * CN + c] + p.gamma * lmu[3], cprev);
+        const float ph = A0.x;
+        const float inc = fmaf(p.dt, fmaf(p.gamma, lm[0].x, q1.y), cprev);
         const float nv = ph + inc;
         phic[g] = inc - (nv - ph);
         ophi[g] = nv;
