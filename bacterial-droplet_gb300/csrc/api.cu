@@ -396,6 +396,293 @@ int pick_form(const ttsh_sim* s) {
   return fused_ok(s) ? 1 : 0;
 }
 
+
+// ---- autotuner ---------------------------------------------------------------------------
+
+// Radix orders of the Stockham plan: radix_plan's (radix 4 first) and its reverse.
+std::vector<std::vector<int>> radix_orders(int N) {
+  std::vector<std::vector<int>> r;
+  const std::vector<int> a = radix_plan(N);
+  r.push_back(a);
+  const std::vector<int> b(a.rbegin(), a.rend());
+  if (b != a) r.push_back(b);
+  return r;
+}
+
+// Mean device time per call of `launch`: `reps` calls captured in a CUDA graph (no host launch
+// gaps between them), best of 3 rounds after one warm-up round; `prep` runs before every round,
+// outside the timed region.
+template <class P, class F>
+double time_graph(cudaStream_t st, int reps, P&& prep, F&& launch) {
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+  try {
+    for (int r = 0; r < reps; ++r) launch();
+  } catch (...) {
+    cudaStreamEndCapture(st, &g);
+    if (g) cudaGraphDestroy(g);
+    throw;
+  }
+  CK(cudaStreamEndCapture(st, &g));
+  cudaGraphExec_t ge = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&ge, g, 0);
+  cudaGraphDestroy(g);
+  CK(ei);
+  cudaEvent_t a = nullptr, b = nullptr;
+  double best = 1e30;
+  try {
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    for (int round = 0; round < 4; ++round) {
+      prep();
+      CK(cudaEventRecord(a, st));
+      CK(cudaGraphLaunch(ge, st));
+      CK(cudaEventRecord(b, st));
+      CK(cudaEventSynchronize(b));
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, a, b));
+      if (round > 0) best = std::min(best, (double)ms / reps);
+    }
+  } catch (...) {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    cudaGraphExecDestroy(ge);
+    throw;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaGraphExecDestroy(ge);
+  return best;
+}
+
+template <class T>
+void upload_group(ttsh_sim* s, Engine<T>& E, size_t gi) {
+  std::vector<InstDev<T>> arr;
+  for (int i : E.members[gi]) arr.push_back(E.h[i]);
+  CK(cudaMemcpyAsync(E.groups[gi].d_inst, arr.data(), sizeof(InstDev<T>) * arr.size(), cudaMemcpyHostToDevice,
+                     s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+}
+
+template <class T>
+void set_radix(ttsh_sim* s, Engine<T>& E, size_t gi, const std::vector<int>& r) {
+  for (int i : E.members[gi]) {
+    E.h[i].nstages = (int)r.size();
+    for (size_t k = 0; k < r.size(); ++k) E.h[i].radix[k] = r[k];
+  }
+  upload_group(s, E, gi);
+}
+
+template <class T>
+void get_tuning(const ttsh_sim* s, const Engine<T>& E, size_t gi, ttsh_tuning* t) {
+  const Group<T>& G = E.groups[gi];
+  const InstDev<T>& I = E.h[E.members[gi][0]];
+  std::memset(t, 0, sizeof(*t));
+  t->N = G.N;
+  t->n = G.n;
+  t->fft_kind = G.fft_kind;
+  t->fft_lb = G.fft_lb;
+  t->nstages = I.nstages;
+  for (int k = 0; k < I.nstages; ++k) t->radix[k] = I.radix[k];
+  for (int k = 0; k < 3; ++k) t->zc[k] = s->fused ? G.zc[k] : 0;
+  for (int k = 0; k < 4; ++k) t->ms[k] = G.tuned_ms[k];
+}
+
+// Checks a configuration against what the kernels support; returns an error message or "".
+template <class T>
+std::string check_tuning(const ttsh_sim* s, const Group<T>& G, const ttsh_tuning& t) {
+  if (t.N != G.N || t.n != G.n) return "tuning: N or group size differs from the group";
+  if (t.fft_kind != 0 && t.fft_kind != 1) return "tuning: fft_kind must be 0 or 1";
+  if (t.fft_lb != 0) {
+    const std::vector<int> c = fft_lb_candidates<T>(G.N);
+    if (std::find(c.begin(), c.end(), t.fft_lb) == c.end()) return "tuning: unsupported Stockham lines per CTA";
+  }
+  if (t.nstages < 1 || t.nstages > 16) return "tuning: bad radix plan length";
+  long prod = 1;
+  for (int k = 0; k < t.nstages; ++k) {
+    const int r = t.radix[k];
+    if (r != 2 && r != 3 && r != 4 && r != 5) return "tuning: radix must be 2, 3, 4 or 5";
+    prod *= r;
+  }
+  if (prod != G.N) return "tuning: radix plan does not multiply to N";
+  if (s->fused)
+    for (int k = 0; k < 3; ++k) {
+      if (t.zc[k] < 1) return "tuning: z-planes per CTA must be >= 1";
+      if ((long)((G.N + t.zc[k] - 1) / t.zc[k]) * G.n > 65535) return "tuning: grid too large";
+    }
+  return "";
+}
+
+template <class T>
+void apply_tuning(ttsh_sim* s, Engine<T>& E, size_t gi, const ttsh_tuning& t) {
+  Group<T>& G = E.groups[gi];
+  G.fft_kind = t.fft_kind;
+  G.fft_lb = t.fft_lb;
+  for (int k = 0; k < 4; ++k) G.tuned_ms[k] = 0;
+  if (s->fused)
+    for (int k = 0; k < 3; ++k) G.zc[k] = t.zc[k];
+  set_radix(s, E, gi, std::vector<int>(t.radix, t.radix + t.nstages));
+}
+
+// Copies of the arrays the trial launches overwrite at the current parity (u, P, the phi
+// compensation, the pressures), restored after the trials.
+template <class T>
+struct TrialBackup {
+  std::vector<std::pair<void*, size_t>> arrays;
+  char* buf = nullptr;
+  void save(ttsh_sim* s, Engine<T>& E, size_t gi) {
+    for (int i : E.members[gi]) {
+      InstDev<T>& I = E.h[i];
+      const size_t n = (size_t)I.N * I.N * I.N;
+      for (int b = 0; b < 3; ++b) arrays.push_back({I.U[b], n * sizeof(T)});
+      for (int b = 0; b < 3; ++b) arrays.push_back({I.P[b], n * sizeof(T)});
+      if (I.phic) arrays.push_back({I.phic, n * sizeof(T)});
+      arrays.push_back({I.W, 2 * n * sizeof(T)});
+    }
+    size_t tot = 0;
+    for (auto& a : arrays) tot += a.second;
+    CK(cudaMalloc(&buf, tot));
+    size_t off = 0;
+    for (auto& a : arrays) {
+      CK(cudaMemcpyAsync(buf + off, a.first, a.second, cudaMemcpyDeviceToDevice, s->stream));
+      off += a.second;
+    }
+  }
+  void restore(ttsh_sim* s) {
+    size_t off = 0;
+    for (auto& a : arrays) {
+      CK(cudaMemcpyAsync(a.first, buf + off, a.second, cudaMemcpyDeviceToDevice, s->stream));
+      off += a.second;
+    }
+    CK(cudaStreamSynchronize(s->stream));
+  }
+  ~TrialBackup() {
+    if (buf) cudaFree(buf);
+  }
+};
+
+template <class T>
+void tune_group(ttsh_sim* s, Engine<T>& E, size_t gi, ttsh_tuning* out) {
+  Group<T>& G = E.groups[gi];
+  const int par = s->par;
+  cudaStream_t st = s->stream;
+  // launches per timed graph: more for small groups (a few microseconds per launch); the FFT
+  // keeps 3 (repeated Poisson solves of one source grow by up to 1/k^2 each)
+  const double sites = (double)G.N * G.N * G.N * G.n;
+  const int reps = std::max(3, std::min(20, (int)(3e7 / sites)));
+  const int reps_fft = 3;
+  TrialBackup<T> bk;
+  bk.save(s, E, gi);
+  try {
+    // the FFT, timed on a fresh Poisson source each time (the divergence launch refills W)
+    auto fill = [&]() {
+      if (s->fused) E.launch_fused_div_t(G, par, st);
+      else launch_div<T>(G, par, st);
+    };
+    auto fft = [&]() {
+      for (int p = 0; p < 5; ++p) launch_fft_pass<T>(G, p, st);
+    };
+    struct Cand { int kind, lb; std::vector<int> radix; };
+    std::vector<Cand> cands;
+    const std::vector<std::vector<int>> orders = radix_orders(G.N);
+    if (fftreg_has<T>(G.N)) cands.push_back({0, 0, orders[0]});
+    for (int lb : fft_lb_candidates<T>(G.N))
+      for (const auto& o : orders) cands.push_back({1, lb, o});
+    double best = 1e30;
+    Cand pick = cands[0];
+    for (const Cand& c : cands) {
+      G.fft_kind = c.kind;
+      G.fft_lb = c.lb;
+      set_radix(s, E, gi, c.radix);
+      const double t = time_graph(st, reps_fft, fill, fft);
+      if (t < best) { best = t; pick = c; }
+    }
+    G.fft_kind = pick.kind;
+    G.fft_lb = pick.lb;
+    set_radix(s, E, gi, pick.radix);
+    double ms[4] = {best, 0, 0, 0};
+    if (s->fused) {
+      const int zcs[] = {8, 16, 32, 64, 128, 256};
+      for (int k = 0; k < 3; ++k) {
+        double bk_t = 1e30;
+        int bk_z = G.zc[k];
+        for (int z : zcs) {
+          if (z > G.N && z != zcs[0]) continue;
+          if ((long)((G.N + z - 1) / z) * G.n > 65535) continue;
+          G.zc[k] = z;
+          const double t = time_graph(st, reps, [] {}, [&] {
+            if (k == 0) E.launch_fused_rhs_t(G, par, st);
+            else if (k == 1) E.launch_fused_div_t(G, par, st);
+            else E.launch_fused_correct_t(G, par, st);
+          });
+          if (t < bk_t) { bk_t = t; bk_z = z; }
+        }
+        G.zc[k] = bk_z;
+        ms[1 + k] = bk_t;
+      }
+    }
+    bk.restore(s);
+    for (int k = 0; k < 4; ++k) G.tuned_ms[k] = ms[k];
+    get_tuning(s, E, gi, out);
+  } catch (...) {
+    try { bk.restore(s); } catch (...) {}
+    throw;
+  }
+}
+
+std::string tune_key(const ttsh_sim* s, int N, int n) {
+  cudaDeviceProp pr{};
+  CK(cudaGetDeviceProperties(&pr, s->device));
+  std::string name = pr.name;
+  for (char& c : name)
+    if (c == ' ' || c == ':') c = '_';
+  char buf[256];
+  std::snprintf(buf, sizeof buf, "%s sm%d%d p%d f%d N%d n%d", name.c_str(), pr.major, pr.minor, s->precision,
+                s->fused ? 1 : 0, N, n);
+  return buf;
+}
+
+// Cache file: one line per entry, "<key> : kind lb zc0 zc1 zc2 nstages radix...".
+std::map<std::string, ttsh_tuning> read_cache(const char* path) {
+  std::map<std::string, ttsh_tuning> m;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return m;
+  char line[1024];
+  while (std::fgets(line, sizeof line, f)) {
+    const char* sep = std::strstr(line, " : ");
+    if (!sep) continue;
+    ttsh_tuning t{};
+    int used = 0;
+    if (std::sscanf(sep + 3, "%d %d %d %d %d %d%n", &t.fft_kind, &t.fft_lb, &t.zc[0], &t.zc[1], &t.zc[2],
+                    &t.nstages, &used) != 6)
+      continue;
+    if (t.nstages < 1 || t.nstages > 16) continue;
+    const char* q = sep + 3 + used;
+    bool ok = true;
+    for (int k = 0; k < t.nstages && ok; ++k) {
+      int u = 0;
+      ok = std::sscanf(q, "%d%n", &t.radix[k], &u) == 1;
+      q += u;
+    }
+    if (ok) m[std::string(line, (size_t)(sep - line))] = t;
+  }
+  std::fclose(f);
+  return m;
+}
+
+void append_cache(const char* path, const std::string& key, const ttsh_tuning& t) {
+  FILE* f = std::fopen(path, "a");
+  if (!f) throw std::runtime_error(std::string("tuning cache: cannot open ") + path);
+  std::string line = key + " : " + std::to_string(t.fft_kind) + " " + std::to_string(t.fft_lb) + " " +
+                     std::to_string(t.zc[0]) + " " + std::to_string(t.zc[1]) + " " + std::to_string(t.zc[2]) + " " +
+                     std::to_string(t.nstages);
+  for (int k = 0; k < t.nstages; ++k) line += " " + std::to_string(t.radix[k]);
+  line += "\n";
+  const bool ok = std::fputs(line.c_str(), f) >= 0;
+  std::fclose(f);
+  if (!ok) throw std::runtime_error(std::string("tuning cache: cannot write ") + path);
+}
+
 }  // namespace
 
 // Host (FP64) <-> device (T) copies of one N^3 field.
@@ -948,6 +1235,66 @@ int ttsh_profile_kernels(ttsh_sim* s, int nsteps, int cap, const char** names, d
     return TTSH_OK;
   });
   return rc ? -rc : written;
+}
+
+int ttsh_num_groups(const ttsh_sim* s) {
+  if (!s) return 0;
+  return s->precision == 32 ? (int)s->ef.groups.size() : (int)s->ed.groups.size();
+}
+
+int ttsh_get_tuning(const ttsh_sim* s, int group, ttsh_tuning* out) {
+  if (!s || !out) return set_error(TTSH_E_INVALID, "null argument");
+  if (group < 0 || group >= ttsh_num_groups(s)) return set_error(TTSH_E_INVALID, "group out of range");
+  if (s->precision == 32) get_tuning(s, s->ef, group, out);
+  else get_tuning(s, s->ed, group, out);
+  return TTSH_OK;
+}
+
+int ttsh_set_tuning(ttsh_sim* s, int group, const ttsh_tuning* in) {
+  if (!s || !in) return set_error(TTSH_E_INVALID, "null argument");
+  if (group < 0 || group >= ttsh_num_groups(s)) return set_error(TTSH_E_INVALID, "group out of range");
+  return guarded([&]() -> int {
+    CK(cudaSetDevice(s->device));
+    std::string err;
+    s->with_engine([&](auto& E) { err = check_tuning(s, E.groups[group], *in); });
+    if (!err.empty()) return set_error(TTSH_E_INVALID, err);
+    CK(cudaStreamSynchronize(s->stream));
+    s->with_engine([&](auto& E) { apply_tuning(s, E, group, *in); });
+    capture_graphs(s);
+    return TTSH_OK;
+  });
+}
+
+int ttsh_autotune(ttsh_sim* s, const char* cache_path) {
+  if (!s) return set_error(TTSH_E_INVALID, "null argument");
+  return guarded([&]() -> int {
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    std::map<std::string, ttsh_tuning> cache;
+    if (cache_path) cache = read_cache(cache_path);
+    int rc = TTSH_OK;
+    s->with_engine([&](auto& E) {
+      for (size_t g = 0; g < E.groups.size() && rc == TTSH_OK; ++g) {
+        const std::string key = tune_key(s, E.groups[g].N, E.groups[g].n);
+        auto it = cache.find(key);
+        if (it != cache.end()) {
+          ttsh_tuning t = it->second;
+          t.N = E.groups[g].N;
+          t.n = E.groups[g].n;
+          const std::string err = check_tuning(s, E.groups[g], t);
+          if (err.empty()) {
+            apply_tuning(s, E, g, t);
+            continue;
+          }
+        }
+        ttsh_tuning t{};
+        tune_group(s, E, g, &t);
+        if (cache_path) append_cache(cache_path, key, t);
+      }
+    });
+    capture_graphs(s);
+    return rc;
+  });
 }
 
 const char* ttsh_strerror(int code) {

@@ -176,7 +176,7 @@ template <class T, int PASS>
 void launch_one(const Group<T>& g, cudaStream_t st) {
   typedef typename CxT<T>::type C;
   const int N = g.N;
-  const int LB = pick_lb(N, sizeof(C));
+  const int LB = fft_lines(g);
   const size_t smem = 2 * (size_t)LB * (N + 1) * sizeof(C);
   const int axis = (PASS == 0 || PASS == 4) ? 0 : ((PASS == 1 || PASS == 3) ? 1 : 2);
   const int nblk = axis == 0 ? (N * N) / LB : N * (N / LB);
@@ -187,11 +187,16 @@ void launch_one(const Group<T>& g, cudaStream_t st) {
 
 }  // namespace
 
+// One kernel serves every size, so its shared-memory limit is only ever raised: a group of one
+// size must not lower the limit another size's launches need.
 template <class T, int PASS>
 void set_attr(int N) {
   typedef typename CxT<T>::type C;
   const size_t smem = 2 * (size_t)pick_lb(N, sizeof(C)) * (N + 1) * sizeof(C);
-  cudaError_t e = cudaFuncSetAttribute(k_fft<T, PASS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncAttributes fa{};
+  cudaError_t e = cudaFuncGetAttributes(&fa, k_fft<T, PASS>);
+  if (e == cudaSuccess && (size_t)fa.maxDynamicSharedSizeBytes >= smem) return;
+  e = cudaFuncSetAttribute(k_fft<T, PASS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) throw std::runtime_error(std::string("fft smem attribute: ") + cudaGetErrorString(e));
 }
 
@@ -203,6 +208,24 @@ void fft_prepare(int N) {
   set_attr<T, 2>(N);
   set_attr<T, 3>(N);
   set_attr<T, 4>(N);
+}
+
+template <class T>
+std::vector<int> fft_lb_candidates(int N) {
+  typedef typename CxT<T>::type C;
+  std::vector<int> r;
+  for (int lb = pick_lb(N, sizeof(C)); lb >= 1; lb >>= 1)
+    if (N % lb == 0) r.push_back(lb);
+  return r;
+}
+
+template <class T>
+int fft_lines(const Group<T>& g) {
+  typedef typename CxT<T>::type C;
+  const int mx = pick_lb(g.N, sizeof(C));  // the shared-memory limit is set for this one
+  if (g.fft_lb == 0) return mx;
+  if (g.fft_lb < 1 || g.fft_lb > mx || g.N % g.fft_lb != 0) throw std::runtime_error("fft: bad lines per CTA");
+  return g.fft_lb;
 }
 
 template <class T>
@@ -224,6 +247,10 @@ void launch_fft_pass(const Group<T>& g, int pass, cudaStream_t st) {
   }
 }
 
+template std::vector<int> fft_lb_candidates<float>(int);
+template std::vector<int> fft_lb_candidates<double>(int);
+template int fft_lines<float>(const Group<float>&);
+template int fft_lines<double>(const Group<double>&);
 template void launch_fft_pass<float>(const Group<float>&, int, cudaStream_t);
 template void launch_fft_pass<double>(const Group<double>&, int, cudaStream_t);
 template size_t fft_smem_bytes<float>(int, int);

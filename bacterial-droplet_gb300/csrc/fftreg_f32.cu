@@ -8,6 +8,10 @@ bool fftreg_launch<float>(const Group<float>& g, int pass, cudaStream_t st) {
   return g.fft_kind == 0 && fftreg::reg_launch<float>(g, pass, st);
 }
 template <>
+bool fftreg_has<float>(int N) {
+  return fftreg::reg_supported<float>(N);
+}
+template <>
 void fftreg_prepare<float>(int N) {
   fftreg::reg_prepare<float>(N);
 }

@@ -8,6 +8,10 @@ bool fftreg_launch<double>(const Group<double>& g, int pass, cudaStream_t st) {
   return g.fft_kind == 0 && fftreg::reg_launch<double>(g, pass, st);
 }
 template <>
+bool fftreg_has<double>(int N) {
+  return fftreg::reg_supported<double>(N);
+}
+template <>
 void fftreg_prepare<double>(int N) {
   fftreg::reg_prepare<double>(N);
 }

@@ -39,7 +39,6 @@ namespace ttsh {
 namespace {
 
 constexpr int TX = 32, TY = 16;   // output tile (columns)
-constexpr int ZC = 64;            // z-planes per block (chunk)
 constexpr int RB = 2;             // strip length (sites per thread) of fused_rhs stage 1
 constexpr int NT = 512;           // threads of fused_rhs: one tile column each in phase 2
 constexpr int US = 4;             // strip length of the velocity terms (phase 1)
@@ -187,15 +186,15 @@ __device__ __forceinline__ V z_part(const V* Z, int W) {
 }
 
 // ------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __restrict__ insts, int par, int nchunk) {
+__global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc) {
   extern __shared__ __align__(16) unsigned char smr[];
   const int N = insts[0].N;
   const InstDev<float>& I = insts[blockIdx.z / nchunk];
   const Phys<float> p = I.ph;  // by value: read once, kept in registers
   const SepK sk{p.c2h * (1.f / 36.f), p.cl12, p.cl23, p.cl143};
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-  const int z0 = (blockIdx.z % nchunk) * ZC;
-  const int z1 = min(z0 + ZC, N);
+  const int z0 = (blockIdx.z % nchunk) * zc;  // zc z-planes per block (a tuning choice)
+  const int z1 = min(z0 + zc, N);
   const size_t NN = (size_t)N * N;
   const float* __restrict__ gphi = I.phi[par];
   const float* __restrict__ gP[3] = {I.P[0], I.P[1], I.P[2]};
@@ -473,12 +472,12 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 
-__global__ void __launch_bounds__(NTC, 2) k_fused_div(const InstDev<float>* __restrict__ insts, int par, int nchunk) {
+__global__ void __launch_bounds__(NTC, 2) k_fused_div(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc) {
   extern __shared__ __align__(16) float sm[];
   const int N = insts[0].N;
   const InstDev<float>& I = insts[blockIdx.z / nchunk];
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-  const int z0 = (blockIdx.z % nchunk) * ZC, z1 = min(z0 + ZC, N);
+  const int z0 = (blockIdx.z % nchunk) * zc, z1 = min(z0 + zc, N);
   const size_t NN = (size_t)N * N;
   const float* cur[6] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2],
                          I.Ps[par ^ 1][0], I.Ps[par ^ 1][1], I.Ps[par ^ 1][2]};
@@ -542,14 +541,14 @@ __global__ void __launch_bounds__(NTC, 2) k_fused_div(const InstDev<float>* __re
   }
 }
 
-__global__ void __launch_bounds__(NTC, 2) k_fused_correct(const InstDev<float>* __restrict__ insts, int par, int nchunk) {
+__global__ void __launch_bounds__(NTC, 2) k_fused_correct(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc) {
   extern __shared__ __align__(16) unsigned char smc[];
   const int N = insts[0].N;
   const InstDev<float>& I = insts[blockIdx.z / nchunk];
   const float kd = I.ph.c2h * (1.f / 36.f);
   const float dt = I.ph.dt;
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-  const int z0 = (blockIdx.z % nchunk) * ZC, z1 = min(z0 + ZC, N);
+  const int z0 = (blockIdx.z % nchunk) * zc, z1 = min(z0 + zc, N);
   const size_t NN = (size_t)N * N;
   const int niter = (z1 - z0) + 2;
   const float* qs[6] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2],
@@ -638,8 +637,9 @@ inline void check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-dim3 grid_for(const Group<float>& g, int& nchunk) {
-  nchunk = (g.N + ZC - 1) / ZC;
+dim3 grid_for(const Group<float>& g, int zc, int& nchunk) {
+  if (zc < 1) throw std::runtime_error("fused: z-planes per block must be >= 1");
+  nchunk = (g.N + zc - 1) / zc;
   if ((long)nchunk * g.n > 65535) throw std::runtime_error("fused: too many droplets in one group");
   return dim3(g.N / TX, g.N / TY, nchunk * g.n);
 }
@@ -659,22 +659,22 @@ void fused_prepare() {
 
 void launch_fused_rhs(const Group<float>& g, int par, cudaStream_t st) {
   int nchunk;
-  dim3 grid = grid_for(g, nchunk);
-  k_fused_rhs<<<grid, NT, RHS_SMEM, st>>>(g.d_inst, par, nchunk);
+  dim3 grid = grid_for(g, g.zc[0], nchunk);
+  k_fused_rhs<<<grid, NT, RHS_SMEM, st>>>(g.d_inst, par, nchunk, g.zc[0]);
   check(cudaGetLastError(), "fused_rhs launch");
 }
 
 void launch_fused_div(const Group<float>& g, int par, cudaStream_t st) {
   int nchunk;
-  dim3 grid = grid_for(g, nchunk);
-  k_fused_div<<<grid, NTC, DIV_SMEM, st>>>(g.d_inst, par, nchunk);
+  dim3 grid = grid_for(g, g.zc[1], nchunk);
+  k_fused_div<<<grid, NTC, DIV_SMEM, st>>>(g.d_inst, par, nchunk, g.zc[1]);
   check(cudaGetLastError(), "fused_div launch");
 }
 
 void launch_fused_correct(const Group<float>& g, int par, cudaStream_t st) {
   int nchunk;
-  dim3 grid = grid_for(g, nchunk);
-  k_fused_correct<<<grid, NTC, COR_SMEM, st>>>(g.d_inst, par, nchunk);
+  dim3 grid = grid_for(g, g.zc[2], nchunk);
+  k_fused_correct<<<grid, NTC, COR_SMEM, st>>>(g.d_inst, par, nchunk, g.zc[2]);
   check(cudaGetLastError(), "fused_correct launch");
 }
 

@@ -55,6 +55,7 @@ int ttsh_struct_size(int which) {
     case 0: return (int)sizeof(ttsh_input);
     case 1: return (int)sizeof(ttsh_ext);
     case 2: return (int)sizeof(ttsh_stats);
+    case 3: return (int)sizeof(ttsh_tuning);
     default: return -1;
   }
 }

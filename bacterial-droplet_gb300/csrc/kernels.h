@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <vector>
+
 namespace ttsh {
 
 template <class T> struct InstDev;
@@ -13,6 +15,9 @@ struct Group {
   int n;               // instances in the group
   int N;
   int fft_kind = 0;    // 0: register-resident FFT kernels where the size has them; 1: Stockham only
+  int fft_lb = 0;      // Stockham lines per CTA (0: the largest power of two that fits)
+  int zc[3] = {64, 64, 64};  // z-planes per CTA of fused_rhs, fused_div, fused_correct
+  double tuned_ms[4] = {0, 0, 0, 0};  // the tuner's timings of this configuration (host record)
   double* red = nullptr;  // FP64 diagnostics partials of the whole group (n x 4 x blocks), contiguous
 };
 
@@ -31,9 +36,13 @@ template <class T> void launch_fft_pass(const Group<T>& g, int pass, cudaStream_
 template <class T> size_t fft_smem_bytes(int N, int pass);
 // Sets the dynamic shared-memory limits of the FFT kernels for size N (call before capture).
 template <class T> void fft_prepare(int N);
+// Stockham lines per CTA: the candidates for size N (largest first) and the one a group uses.
+template <class T> std::vector<int> fft_lb_candidates(int N);
+template <class T> int fft_lines(const Group<T>& g);
 // Register-resident FFT passes (fftreg_*.cu): false when the size has none (Stockham is used).
 template <class T> bool fftreg_launch(const Group<T>& g, int pass, cudaStream_t st);
 template <class T> void fftreg_prepare(int N);
+template <class T> bool fftreg_has(int N);
 
 // Fused FP32 form (fused.cu): rhs (u*, P*, phi'), div (packed Poisson source), correct (u, P).
 void launch_fused_rhs(const Group<float>& g, int par, cudaStream_t st);

@@ -55,6 +55,30 @@ class Stats(ctypes.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
 
 
+class Tuning(ctypes.Structure):
+    """ttsh_tuning: the kernel configuration of one group of equal-N droplets."""
+    _fields_ = [("N", ctypes.c_int), ("n", ctypes.c_int), ("fft_kind", ctypes.c_int), ("fft_lb", ctypes.c_int),
+                ("nstages", ctypes.c_int), ("radix", ctypes.c_int * 16), ("zc", ctypes.c_int * 3),
+                ("ms", ctypes.c_double * 4)]
+
+    def as_dict(self):
+        return {"N": self.N, "n": self.n, "fft_kind": self.fft_kind, "fft_lb": self.fft_lb,
+                "radix": list(self.radix[:self.nstages]), "zc": list(self.zc),
+                "ms": {"fft": self.ms[0], "fused_rhs": self.ms[1], "fused_div": self.ms[2],
+                       "fused_correct": self.ms[3]}}
+
+    @classmethod
+    def from_dict(cls, d):
+        t = cls()
+        t.N, t.n, t.fft_kind, t.fft_lb = d["N"], d["n"], d["fft_kind"], d["fft_lb"]
+        t.nstages = len(d["radix"])
+        for k, r in enumerate(d["radix"]):
+            t.radix[k] = r
+        for k, z in enumerate(d["zc"]):
+            t.zc[k] = z
+        return t
+
+
 class TTSHError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__("%s (%d): %s" % (_strerror(code), code, msg))
@@ -111,6 +135,10 @@ def lib():
                                ctypes.c_int], ctypes.c_int),
             "ttsh_snapshot_slice": ([_VP, ctypes.c_int, _D, ctypes.POINTER(ctypes.c_int), _D], ctypes.c_int),
             "ttsh_load_checkpoint": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),
+            "ttsh_num_groups": ([_VP], ctypes.c_int),
+            "ttsh_get_tuning": ([_VP, ctypes.c_int, ctypes.POINTER(Tuning)], ctypes.c_int),
+            "ttsh_set_tuning": ([_VP, ctypes.c_int, ctypes.POINTER(Tuning)], ctypes.c_int),
+            "ttsh_autotune": ([_VP, ctypes.c_char_p], ctypes.c_int),
             "ttsh_step_noalloc": ([ctypes.POINTER(Input), ctypes.POINTER(Ext), ctypes.c_int] + [_VP] * 7 + [_VP],
                                   ctypes.c_int),
         }
@@ -325,6 +353,24 @@ class Sim:
 
     def launches_per_step(self) -> int:
         return lib().ttsh_launches_per_step(self._h)
+
+    def tuning(self):
+        """The kernel configuration of every group of equal-N droplets (list of dicts)."""
+        out = []
+        for g in range(lib().ttsh_num_groups(self._h)):
+            t = Tuning()
+            _check(lib().ttsh_get_tuning(self._h, g, ctypes.byref(t)))
+            out.append(t.as_dict())
+        return out
+
+    def set_tuning(self, group: int, cfg: dict):
+        _check(lib().ttsh_set_tuning(self._h, group, ctypes.byref(Tuning.from_dict(cfg))))
+
+    def autotune(self, cache: str = None):
+        """Times the kernel candidates of every group on the current fields and keeps the fastest
+        (the state is left as it was); returns the chosen configurations with their timings."""
+        _check(lib().ttsh_autotune(self._h, None if cache is None else cache.encode()))
+        return self.tuning()
 
     def profile_kernels(self, nsteps: int):
         cap = 16

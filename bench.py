@@ -251,6 +251,7 @@ def main():
     ap.add_argument("--form", type=int, default=0, choices=[0, 1, 2], help="0 auto, 1 plain, 2 fused")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default kernel configuration")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
@@ -281,6 +282,9 @@ def main():
     states = init_states(ttsh, drops, pinned=False)
     for i, (phi, P, u, _) in enumerate(states):
         sim.set_state(i, phi, P, u)
+    # kernel configuration per droplet size (FFT kind / lines / radix order, z-planes per CTA of
+    # the fused kernels), timed on these fields before the warm-up
+    tuning = None if args.no_tune else sim.autotune()
     sim.step(args.warmup)
     torch.cuda.synchronize()
 
@@ -359,7 +363,11 @@ def main():
                 "droplets": len(drops), "sites_per_gpu": sites, "form": "fused" if "fused_rhs" in prof else "plain",
                 "physics": "reference (continuous k^2, stale-halo divergence)" if args.k2 == 0 else "discrete k^2",
                 "l2": "inputs larger than L2 (%.1f GB of fields per GPU)" % (sites * 22 * wbytes / 1e9),
-                "parallelism": "replicas" if world > 1 else "1 GPU"},
+                "parallelism": "replicas" if world > 1 else "1 GPU",
+                "tuning": "default" if tuning is None else [
+                    "N=%d x%d: fft %s, zc %s" % (t["N"], t["n"], "register" if t["fft_kind"] == 0 else
+                                                 "stockham lb=%d radix=%s" % (t["fft_lb"], t["radix"]), t["zc"])
+                    for t in tuning]},
             "hbm_pct_of_step": 100 * hbm_frac,
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,

@@ -198,9 +198,42 @@ double ttsh_time(const ttsh_sim* s);
 int ttsh_profile_kernels(ttsh_sim* s, int nsteps, int cap, const char** names, double* ms_per_step,
                          int64_t* launches_per_step);
 
-/* sizeof(ttsh_input) for which == 0, sizeof(ttsh_ext) for 1, sizeof(ttsh_stats) for 2, else -1:
- * lets a caller that re-declares the structures (the TTSH3D.cu shim) check the layout. */
+/* sizeof(ttsh_input) for which == 0, sizeof(ttsh_ext) for 1, sizeof(ttsh_stats) for 2,
+ * sizeof(ttsh_tuning) for 3, else -1: lets a caller that re-declares the structures (the
+ * TTSH3D.cu shim) check the layout. */
 int ttsh_struct_size(int which);
+
+/* Autotuner — no counterpart in the reference (whose tile shapes are fixed by its launch
+ * configuration, TTSH3D.cu:224-235, and whose FFT plan is cuFFT's, :1123). The choices are made
+ * per group of droplets of equal N (one launch per kernel per group):
+ *   the FFT: register-resident passes (where the size has them) or the shared-memory Stockham
+ *   passes, with their lines per CTA and the order of the radix plan;
+ *   the fused FP32 kernels: the z-extent of a CTA's tile (z-planes per CTA) of each of the three.
+ * None of them changes results except the FFT choice (rounding order only). */
+typedef struct {
+  int N;           /* droplet size of the group */
+  int n;           /* droplets in the group */
+  int fft_kind;    /* 0 register-resident passes where the size has them, 1 Stockham */
+  int fft_lb;      /* Stockham lines per CTA; 0 = the largest that fits */
+  int nstages;     /* Stockham radix plan: radix[0..nstages-1], each 2, 3, 4 or 5, product N */
+  int radix[16];
+  int zc[3];       /* z-planes per CTA of fused_rhs, fused_div, fused_correct (fused form) */
+  double ms[4];    /* measured per launch: FFT (5 passes), fused_rhs, fused_div, fused_correct;
+                      0 where not measured (taken from a cache, or set by the caller) */
+} ttsh_tuning;
+
+/* Number of groups (distinct N) of the instance. */
+int ttsh_num_groups(const ttsh_sim* s);
+/* The configuration group `group` runs with. */
+int ttsh_get_tuning(const ttsh_sim* s, int group, ttsh_tuning* out);
+/* Applies a configuration to group `group` (N and n must match the group); TTSH_E_INVALID for
+ * a configuration the kernels do not support. Takes effect from the next step. */
+int ttsh_set_tuning(ttsh_sim* s, int group, const ttsh_tuning* in);
+/* Times the candidates of every group on the instance's own fields and keeps the fastest. The
+ * state (phi, P, u, u*, P*, the pressures and T) is left as it was. With cache_path non-NULL,
+ * groups with an entry for this GPU, precision, form, N and group size in that text file take
+ * it without timing, and the choices of the others are appended to it. */
+int ttsh_autotune(ttsh_sim* s, const char* cache_path);
 
 /* Launch count of one step (kernels of this library). */
 int ttsh_launches_per_step(const ttsh_sim* s);

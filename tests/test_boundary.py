@@ -181,3 +181,13 @@ def test_readdraw_restatement_matches_op_py():
     u = rng.standard_normal((12, 16))
     np.testing.assert_allclose(RD.d1xO4(u, 0.7), op.d1xO4(u, 0.7), rtol=0, atol=1e-13)
     np.testing.assert_allclose(RD.d1yO4(u, 0.7), op.d1yO4(u, 0.7), rtol=0, atol=1e-13)
+
+
+def test_struct_layouts_match_the_library():
+    """ctypes mirrors of ttsh_input, ttsh_ext, ttsh_stats, ttsh_tuning have the library's sizes."""
+    import ctypes
+    import ttsh
+    L = ttsh.lib()
+    for k, cls in enumerate((ttsh.Input, ttsh.Ext, ttsh.Stats, ttsh.Tuning)):
+        assert L.ttsh_struct_size(k) == ctypes.sizeof(cls), cls.__name__
+    assert L.ttsh_struct_size(4) == -1

@@ -91,6 +91,25 @@ def test_batch_uneven_sizes_match_single_runs():
             assert np.array_equal(batch[i][k], single[k]), (i, k)
 
 
+def test_batch_of_stockham_sizes_match_single_runs():
+    """Sizes served only by the Stockham FFT kernel (one kernel for all sizes, with a shared-memory
+    limit per kernel): the larger size must still launch after the smaller one is set up."""
+    import ttsh
+    sizes = [40, 20, 40]
+    states = [random_state(N, seed=200 + i) for i, N in enumerate(sizes)]
+    exts = [ttsh.default_ext(precision=64, zeta=0.01) for _ in sizes]
+    inps = [ttsh.default_input(Nx=N, Ny=N, Nz=N) for N in sizes]
+    with ttsh.Sim(inps, exts) as s:
+        for i, st in enumerate(states):
+            s.set_state(i, st["phi"], st["P"], st["u"], st["us"], st["ps"])
+        s.step(3)
+        batch = [s.get_state(i) for i in range(len(sizes))]
+    for i, st in enumerate(states):
+        single = run_gpu(st, 3, 64, zeta=0.01)
+        for k in ("phi", "P", "u", "pv", "pp"):
+            assert np.array_equal(batch[i][k], single[k]), (i, k)
+
+
 def test_stats_and_watchdog():
     import ttsh
     N = 16
