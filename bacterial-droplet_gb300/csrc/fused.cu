@@ -154,37 +154,6 @@ __device__ __forceinline__ void sep_rows(const LD& ld, const SepK& k, V* dx, V* 
   }
 }
 
-// Plane partial sums of the outer stencils over a product plane, at one column (F points at it):
-//   Laplacian: an off-centre plane adds G = l12 (its 4 diagonal sites) + l23 (its centre site),
-//   the centre plane adds H = l23 (its 4 edge sites) - l143 (its centre site);
-//   divergence: X = delta_x s_y, Y = s_x delta_y (weight s_z over the planes), Z = s_x s_y
-//   (weight delta_z).
-template <class V>
-__device__ __forceinline__ void lap_part(const V* F, int W, const SepK& k, V& G, V& H) {
-  const V v11 = F[0];
-  const V dg = vadd(vadd(F[-W - 1], F[-W + 1]), vadd(F[W - 1], F[W + 1]));
-  const V ed = vadd(vadd(F[-W], F[W]), vadd(F[-1], F[1]));
-  G = vfma(vsplat(k.l12, V()), dg, vmul(vsplat(k.l23, V()), v11));
-  H = vfma(vsplat(k.l23, V()), ed, vmul(vsplat(-k.l143, V()), v11));
-}
-template <class V>
-__device__ __forceinline__ V x_part(const V* X, int W) {
-  const V four = vsplat(4.f, V());
-  return vsub(vfma(four, X[1], vadd(X[-W + 1], X[W + 1])), vfma(four, X[-1], vadd(X[-W - 1], X[W - 1])));
-}
-template <class V>
-__device__ __forceinline__ V y_part(const V* Y, int W) {
-  return vfma(vsplat(4.f, V()), vsub(Y[W], Y[-W]), vadd(vsub(Y[W - 1], Y[-W - 1]), vsub(Y[W + 1], Y[-W + 1])));
-}
-template <class V>
-__device__ __forceinline__ V z_part(const V* Z, int W) {
-  const V four = vsplat(4.f, V());
-  const V t0 = vfma(four, Z[-1], vadd(Z[-W - 1], Z[W - 1]));
-  const V t1 = vfma(four, Z[0], vadd(Z[-W], Z[W]));
-  const V t2 = vfma(four, Z[1], vadd(Z[-W + 1], Z[W + 1]));
-  return vfma(four, t1, vadd(t0, t2));
-}
-
 // ------------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc) {
   extern __shared__ __align__(16) unsigned char smr[];
@@ -238,24 +207,38 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
     }
     cp_async_commit();
   };
-  // the tile column of this thread in phase 2
-  const int qx = tid % TX, qy = tid / TX;
-  const size_t gc = (size_t)(y0 + qy) * N + (x0 + qx);
-  const int qo = (qy + 1) * BW + (qx + 1);  // its B-region index
-  // z-combinations carried from plane to plane (phase 2): for the Laplacians of (mu_0, mu_x),
-  // (mu_y, mu_z), rL1 = the partial sum of the plane just finished + 1, rL2 = that of the plane
-  // after it; likewise rD1 / rD2 for the stress divergence of columns (y, z) and x
-  float2 rL1[2] = {f2(0.f, 0.f), f2(0.f, 0.f)}, rL2[2] = {f2(0.f, 0.f), f2(0.f, 0.f)};
-  float2 rD1 = f2(0.f, 0.f), rD2 = f2(0.f, 0.f);
-  float rX1 = 0.f, rX2 = 0.f;
+  // phase 2: thread tid takes the 2-site strip s = tid % 256 of the tile (column px, rows py0,
+  // py0 + 1) for one half of the outer stencils: half A (tid < 256) the Laplacians of (mu_0, mu_x),
+  // (mu_y, mu_z) and the divergence of stress column x, then P*, phi' and u*_x; half B the
+  // divergence of stress columns (y, z), then u*_y, u*_z. Each half has every input of what it
+  // writes. The sites' rows share a 4 x 3 window of each product plane.
+  static_assert(NT == 2 * TX * (TY / 2), "phase 2: two halves of 2-site strips");
+  const bool halfA = tid < NT / 2;
+  const int ps = tid & (NT / 2 - 1);
+  const int px = ps % TX, py0 = (ps / TX) * 2;
+  const int pbase = py0 * BW + px;  // B index of window row 0 (site 0's row - 1), column px - 1 + 1 - 1
+  // z-combinations carried from plane to plane: for a Laplacian, the partial sum of the plane
+  // just finished + 1 and that of the plane after it (rL1, rL2); likewise for the divergences.
+  // Half A: cv2[0..3] = rL1 [site][pair], cv2[4..7] = rL2, cv1[0..1] = rX1 [site], cv1[2..3] = rX2;
+  // half B: cv2[0..1] = rD1 [site], cv2[2..3] = rD2.
+  float2 cv2[8];
+  float cv1[4];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) cv2[k] = f2(0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) cv1[k] = 0.f;
   issue(0);
   for (int i = 0; i < niter; ++i) {
     cp_async_wait_all();
     __syncthreads();
     if (i + 1 < niter) issue(i + 1);
-    // the phi compensation of this iteration's output site, loaded before phase 1 so that the
-    // phase-1 work covers the load
-    const float cprev = i >= 4 ? phic[(size_t)(z0 - 4 + i) * NN + gc] : 0.f;
+    // the phi compensation of this iteration's output sites (half A), loaded before phase 1 so
+    // that the phase-1 work covers the load
+    float cprev[2] = {0.f, 0.f};
+    if (i >= 4 && halfA) {
+#pragma unroll
+      for (int k = 0; k < 2; ++k) cprev[k] = phic[(size_t)(z0 - 4 + i) * NN + (size_t)(y0 + py0 + k) * N + (x0 + px)];
+    }
     // ---- phase 1a, stage 1 at plane b = z0 - 3 + i over B (tile+1): the products mu_0, mu_b,
     //      S_ab that phase 2 differentiates, and on the tile the pointwise parts of the update
     if (i >= 2 && tid < NS1) {
@@ -379,67 +362,138 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
       }
     }
     __syncthreads();
-    // ---- phase 2, one tile column per thread: the in-plane partial sums of the outer stencils
-    //      over the products of plane b, carried in z; plane c = b - 1 is then complete
+    // ---- phase 2: the in-plane partial sums of the outer stencils over the products of plane
+    //      b, carried in z; plane c = b - 1 is then complete
     if (i >= 2) {
-      float2 lm[2];
+      const int zc = z0 - 4 + i;
+      const float2* pq = sQ + ((i + 1) & 1) * NPQ * CN;     // plane c: stage 1 + velocity terms
+      const int sl = (i + RU - 1) % RU;                     // u at plane c
+      const float2* ac = sA + ((i + RA - 2) % RA) * 2 * AN;  // phi, P at plane c
+      const float2 four = f2(4.f, 4.f);
+      if (halfA) {
+        float2 lm[2][2];  // [site]: (L mu_0, L mu_x), (L mu_y, L mu_z)
 #pragma unroll
-      for (int q = 0; q < 2; ++q) {
-        float2 G, H;
-        lap_part(sPr + (PM0 + q) * BN + qo, BW, sk, G, H);
-        lm[q] = vadd(rL1[q], G);
-        rL1[q] = vadd(rL2[q], H);
-        rL2[q] = G;
-      }
-      // divergence columns (y, z): X of T0, Y of T1, Z of T2 (packed)
-      const float2 Q = vadd(x_part(sPr + PT0 * BN + qo, BW), y_part(sPr + PT1 * BN + qo, BW));
-      const float2 Zr = z_part(sPr + PT2 * BN + qo, BW);
-      const float2 dvyz = vadd(vadd(rD1, Q), Zr);
-      rD1 = vfma(vsplat(4.f, float2()), Q, rD2);
-      rD2 = vsub(Q, Zr);
-      // divergence column x: X of S_xx (T3.x), Y of S_yx (T3.y), Z of S_zx
-      float dvx;
-      {
-        const float2* T = sPr + PT3 * BN + qo;
-        const float2 tmm = T[-BW - 1], tm0 = T[-BW], tmp = T[-BW + 1], t0m = T[-1], t0p = T[1];
-        const float2 tpm = T[BW - 1], tp0 = T[BW], tpp = T[BW + 1];
-        const float xr = fmaf(4.f, t0p.x, tmp.x + tpp.x) - fmaf(4.f, t0m.x, tmm.x + tpm.x);
-        const float yr = fmaf(4.f, tp0.y - tm0.y, (tpm.y - tmm.y) + (tpp.y - tmp.y));
-        const float zr = z_part(sSzx + qo, BW);
-        const float Qx = xr + yr;
-        dvx = rX1 + Qx + zr;
-        rX1 = fmaf(4.f, Qx, rX2);
-        rX2 = Qx - zr;
-      }
-      if (i >= 4) {
-        const int zc = z0 - 4 + i;
-        const float2* pq = sQ + ((i + 1) & 1) * NPQ * CN;  // plane c: stage 1 + velocity terms
-        const int sl = (i + RU - 1) % RU;                  // u at plane c
-        const float2* ac = sA + ((i + RA - 2) % RA) * 2 * AN;  // phi, P at plane c
-        const int c = qy * TX + qx, oa = (qy + 2) * AW + (qx + 2);
-        const size_t g = (size_t)zc * NN + gc;
-        const float2 q0 = pq[0 * CN + c], q1 = pq[1 * CN + c], q2 = pq[2 * CN + c], q3 = pq[3 * CN + c];
-        const float2 uxy = sU01[sl * BN + qo];
-        const float uz = sU2[sl * BN + qo];
-        const float2 A0 = ac[oa], A1 = ac[AN + oa];
-        // u*_b = u_b + dt d/dt u_b (:480-482)
-        oUs[0][g] = fmaf(p.dt, fmaf(sk.d, dvx, q0.x), uxy.x);
-        const float2 us = vfma(vsplat(p.dt, float2()), vfma(vsplat(sk.d, float2()), dvyz, f2(q0.y, q1.x)), f2(uxy.y, uz));
-        oUs[1][g] = us.x;
-        oUs[2][g] = us.y;
-        // P*_b = P_b + dt (pointwise part + eta L mu_b) (:623-629, :486-488)
-        oPs[0][g] = fmaf(p.dt, fmaf(p.eta, lm[0].y, q2.x), A0.y);
-        const float2 ps = vfma(vsplat(p.dt, float2()), vfma(vsplat(p.eta, float2()), lm[1], f2(q2.y, q3.x)), A1);
-        oPs[1][g] = ps.x;
-        oPs[2][g] = ps.y;
-        // phi' = phi + dt (-u.D phi + gamma L mu_0) (:631, :515), compensated: the part of the
-        // increment that rounding drops from phi is carried to the next step (otherwise
-        // increments below half an ulp of phi are lost, a systematic mass drift)
-        const float ph = A0.x;
-        const float inc = fmaf(p.dt, fmaf(p.gamma, lm[0].x, q1.y), cprev);
-        const float nv = ph + inc;
-        phic[g] = inc - (nv - ph);
-        ophi[g] = nv;
+        for (int q = 0; q < 2; ++q) {
+          const float2* F = sPr + (PM0 + q) * BN + pbase;
+          float2 v[4][3];
+#pragma unroll
+          for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) v[r][c] = F[r * BW + c];
+#pragma unroll
+          for (int k = 0; k < 2; ++k) {
+            const float2 ce = v[k + 1][1];
+            const float2 dg = vadd(vadd(v[k][0], v[k][2]), vadd(v[k + 2][0], v[k + 2][2]));
+            const float2 ed = vadd(vadd(v[k][1], v[k + 2][1]), vadd(v[k + 1][0], v[k + 1][2]));
+            const float2 G = vfma(vsplat(sk.l12, float2()), dg, vmul(vsplat(sk.l23, float2()), ce));
+            const float2 H = vfma(vsplat(sk.l23, float2()), ed, vmul(vsplat(-sk.l143, float2()), ce));
+            lm[k][q] = vadd(cv2[k * 2 + q], G);
+            cv2[k * 2 + q] = vadd(cv2[4 + k * 2 + q], H);
+            cv2[4 + k * 2 + q] = G;
+          }
+        }
+        // divergence column x: X of S_xx (T3.x), Y of S_yx (T3.y), Z of S_zx
+        float dvx[2];
+        {
+          const float2* T = sPr + PT3 * BN + pbase;
+          const float* Zs = sSzx + pbase;
+          float2 t[4][3];
+          float z[4][3];
+#pragma unroll
+          for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              t[r][c] = T[r * BW + c];
+              z[r][c] = Zs[r * BW + c];
+            }
+#pragma unroll
+          for (int k = 0; k < 2; ++k) {
+            const float xr = fmaf(4.f, t[k + 1][2].x, t[k][2].x + t[k + 2][2].x) -
+                             fmaf(4.f, t[k + 1][0].x, t[k][0].x + t[k + 2][0].x);
+            const float yr = fmaf(4.f, t[k + 2][1].y - t[k][1].y,
+                                  (t[k + 2][0].y - t[k][0].y) + (t[k + 2][2].y - t[k][2].y));
+            const float z0c = fmaf(4.f, z[k + 1][0], z[k][0] + z[k + 2][0]);
+            const float z1c = fmaf(4.f, z[k + 1][1], z[k][1] + z[k + 2][1]);
+            const float z2c = fmaf(4.f, z[k + 1][2], z[k][2] + z[k + 2][2]);
+            const float zr = fmaf(4.f, z1c, z0c + z2c);
+            const float Qx = xr + yr;
+            dvx[k] = cv1[k] + Qx + zr;
+            cv1[k] = fmaf(4.f, Qx, cv1[2 + k]);
+            cv1[2 + k] = Qx - zr;
+          }
+        }
+        if (i >= 4) {
+#pragma unroll
+          for (int k = 0; k < 2; ++k) {
+            const int c = (py0 + k) * TX + px, oa = (py0 + k + 2) * AW + (px + 2), ob = (py0 + k + 1) * BW + (px + 1);
+            const size_t g = (size_t)zc * NN + (size_t)(y0 + py0 + k) * N + (x0 + px);
+            const float2 q0 = pq[0 * CN + c], q1 = pq[1 * CN + c], q2 = pq[2 * CN + c], q3 = pq[3 * CN + c];
+            const float2 A0 = ac[oa], A1 = ac[AN + oa];
+            // u*_x = u_x + dt d/dt u_x (:480-482)
+            oUs[0][g] = fmaf(p.dt, fmaf(sk.d, dvx[k], q0.x), sU01[sl * BN + ob].x);
+            // P*_b = P_b + dt (pointwise part + eta L mu_b) (:623-629, :486-488)
+            oPs[0][g] = fmaf(p.dt, fmaf(p.eta, lm[k][0].y, q2.x), A0.y);
+            const float2 ps2 = vfma(vsplat(p.dt, float2()), vfma(vsplat(p.eta, float2()), lm[k][1], f2(q2.y, q3.x)), A1);
+            oPs[1][g] = ps2.x;
+            oPs[2][g] = ps2.y;
+            // phi' = phi + dt (-u.D phi + gamma L mu_0) (:631, :515), compensated: the part of
+            // the increment that rounding drops from phi is carried to the next step (otherwise
+            // increments below half an ulp of phi are lost, a systematic mass drift)
+            const float ph = A0.x;
+            const float inc = fmaf(p.dt, fmaf(p.gamma, lm[k][0].x, q1.y), cprev[k]);
+            const float nv = ph + inc;
+            phic[g] = inc - (nv - ph);
+            ophi[g] = nv;
+          }
+        }
+      } else {
+        // divergence columns (y, z), packed: X of T0 = (S_xy, S_xz), Y of T1 = (S_yy, S_yz),
+        // Z of T2 = (S_zy, S_zz)
+        float2 dv[2];
+        {
+          const float2* X = sPr + PT0 * BN + pbase;
+          const float2* Y = sPr + PT1 * BN + pbase;
+          const float2* Z = sPr + PT2 * BN + pbase;
+          float2 xa[4][2], ya[4][3], za[4][3];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            xa[r][0] = X[r * BW];
+            xa[r][1] = X[r * BW + 2];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              ya[r][c] = Y[r * BW + c];
+              za[r][c] = Z[r * BW + c];
+            }
+          }
+#pragma unroll
+          for (int k = 0; k < 2; ++k) {
+            const float2 xr = vsub(vfma(four, xa[k + 1][1], vadd(xa[k][1], xa[k + 2][1])),
+                                   vfma(four, xa[k + 1][0], vadd(xa[k][0], xa[k + 2][0])));
+            const float2 yr = vfma(four, vsub(ya[k + 2][1], ya[k][1]),
+                                   vadd(vsub(ya[k + 2][0], ya[k][0]), vsub(ya[k + 2][2], ya[k][2])));
+            const float2 t0 = vfma(four, za[k + 1][0], vadd(za[k][0], za[k + 2][0]));
+            const float2 t1 = vfma(four, za[k + 1][1], vadd(za[k][1], za[k + 2][1]));
+            const float2 t2 = vfma(four, za[k + 1][2], vadd(za[k][2], za[k + 2][2]));
+            const float2 zr = vfma(four, t1, vadd(t0, t2));
+            const float2 Q = vadd(xr, yr);
+            dv[k] = vadd(vadd(cv2[k], Q), zr);
+            cv2[k] = vfma(four, Q, cv2[2 + k]);
+            cv2[2 + k] = vsub(Q, zr);
+          }
+        }
+        if (i >= 4) {
+#pragma unroll
+          for (int k = 0; k < 2; ++k) {
+            const int c = (py0 + k) * TX + px, ob = (py0 + k + 1) * BW + (px + 1);
+            const size_t g = (size_t)zc * NN + (size_t)(y0 + py0 + k) * N + (x0 + px);
+            const float2 q0 = pq[0 * CN + c], q1 = pq[1 * CN + c];
+            // (u*_y, u*_z) = (u_y, u_z) + dt d/dt (u_y, u_z) (:480-482)
+            const float2 us = vfma(vsplat(p.dt, float2()), vfma(vsplat(sk.d, float2()), dv[k], f2(q0.y, q1.x)),
+                                   f2(sU01[sl * BN + ob].y, sU2[sl * BN + ob]));
+            oUs[1][g] = us.x;
+            oUs[2][g] = us.y;
+          }
+        }
       }
     }
   }
