@@ -184,26 +184,46 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
   // issue(i): A plane a = z0 - 2 + i (phi, P over tile+2) into A slot i % RA, and u plane a - 1
   // (tile+1) into u slot i % RU. Iteration i runs stage 1 at plane b = a - 1 and finishes plane
   // c = a - 2; issue(i + 1) runs during iteration i.
+  // Offsets within a plane of the elements this thread copies (t = tid + k NT of the A region,
+  // tile+2, and of the B region, tile+1), with the periodic wrap: the same for every plane.
+  constexpr int KA = (AN + NT - 1) / NT, KB = (BN + NT - 1) / NT;
+  int offA[KA], offB[KB];
+#pragma unroll
+  for (int k = 0; k < KA; ++k) {
+    const int t = tid + k * NT;
+    offA[k] = t < AN ? wrapN(y0 - 2 + t / AW, N) * N + wrapN(x0 - 2 + t % AW, N) : 0;
+  }
+#pragma unroll
+  for (int k = 0; k < KB; ++k) {
+    const int t = tid + k * NT;
+    offB[k] = t < BN ? wrapN(y0 - 1 + t / BW, N) * N + wrapN(x0 - 1 + t % BW, N) : 0;
+  }
   auto issue = [&](int i) {
-    const int za = ((z0 - 2 + i) % N + N) % N;
+    const size_t za = (size_t)wrapN(z0 - 2 + i, N) * NN;
     float* dst = reinterpret_cast<float*>(sA + (i % RA) * 2 * AN);
-    for (int t = tid; t < AN; t += NT) {
-      const int ay = t / AW, ax = t - ay * AW;
-      const size_t g = (size_t)za * NN + (size_t)wrapN(y0 - 2 + ay, N) * N + wrapN(x0 - 2 + ax, N);
-      cp_async4(dst + 2 * t, gphi + g);
-      cp_async4(dst + 2 * t + 1, gP[0] + g);
-      cp_async4(dst + 2 * (AN + t), gP[1] + g);
-      cp_async4(dst + 2 * (AN + t) + 1, gP[2] + g);
+#pragma unroll
+    for (int k = 0; k < KA; ++k) {
+      const int t = tid + k * NT;
+      if (t < AN) {
+        const size_t g = za + offA[k];
+        cp_async4(dst + 2 * t, gphi + g);
+        cp_async4(dst + 2 * t + 1, gP[0] + g);
+        cp_async4(dst + 2 * (AN + t), gP[1] + g);
+        cp_async4(dst + 2 * (AN + t) + 1, gP[2] + g);
+      }
     }
-    const int zu = ((z0 - 3 + i) % N + N) % N;
+    const size_t zu = (size_t)wrapN(z0 - 3 + i, N) * NN;
     float* du = reinterpret_cast<float*>(sU01 + (i % RU) * BN);
     float* dz = sU2 + (i % RU) * BN;
-    for (int t = tid; t < BN; t += NT) {
-      const int by = t / BW, bx = t - by * BW;
-      const size_t g = (size_t)zu * NN + (size_t)wrapN(y0 - 1 + by, N) * N + wrapN(x0 - 1 + bx, N);
-      cp_async4(du + 2 * t, gU[0] + g);
-      cp_async4(du + 2 * t + 1, gU[1] + g);
-      cp_async4(dz + t, gU[2] + g);
+#pragma unroll
+    for (int k = 0; k < KB; ++k) {
+      const int t = tid + k * NT;
+      if (t < BN) {
+        const size_t g = zu + offB[k];
+        cp_async4(du + 2 * t, gU[0] + g);
+        cp_async4(du + 2 * t + 1, gU[1] + g);
+        cp_async4(dz + t, gU[2] + g);
+      }
     }
     cp_async_commit();
   };
