@@ -47,6 +47,11 @@ constexpr int US = 4;             // strip length of the velocity terms (phase 1
 constexpr int AW = TX + 4, AH = TY + 4, AN = AW * AH;
 constexpr int BW = TX + 2, BH = TY + 2, BN = BW * BH;
 constexpr int CN = TX * TY;
+// Row pitches in shared memory, one element longer than the rows: warps whose lanes sit in
+// different rows (the stage-1 strips of the last two B columns) then hit different banks.
+constexpr int AP = AW + 1, ANP = AP * AH;  // A region (float2 pairs)
+constexpr int BP = BW + 1, BNP = BP * BH;  // B region
+constexpr int CP = TX + 1, CNP = CP * TY;  // the tile (partials)
 // Products of one plane on B, as float2 pairs (plus one scalar field):
 //   M0 = (mu_0, mu_x), M1 = (mu_y, mu_z)       Laplacians: phi', P*
 //   T0 = (S_xy, S_xz), T1 = (S_yy, S_yz), T2 = (S_zy, S_zz)   divergence columns y, z
@@ -60,12 +65,12 @@ constexpr int NPQ = 4;
 // stencils read: the next plane is copied into it (cp.async) while the current ones compute.
 constexpr int RA = 4, RU = 4;
 constexpr size_t OFF_A = 0;
-constexpr size_t OFF_U01 = OFF_A + (size_t)RA * 2 * AN * sizeof(float2);
-constexpr size_t OFF_U2 = OFF_U01 + (size_t)RU * BN * sizeof(float2);
-constexpr size_t OFF_PR = OFF_U2 + (size_t)RU * BN * sizeof(float);
-constexpr size_t OFF_SZX = OFF_PR + (size_t)NPR * BN * sizeof(float2);
-constexpr size_t OFF_PQ = OFF_SZX + (size_t)BN * sizeof(float);
-constexpr size_t RHS_SMEM = OFF_PQ + (size_t)2 * NPQ * CN * sizeof(float2);
+constexpr size_t OFF_U01 = OFF_A + (size_t)RA * 2 * ANP * sizeof(float2);
+constexpr size_t OFF_U2 = OFF_U01 + (size_t)RU * BNP * sizeof(float2);
+constexpr size_t OFF_PR = OFF_U2 + (((size_t)RU * BNP * sizeof(float) + 15) / 16) * 16;
+constexpr size_t OFF_SZX = OFF_PR + (size_t)NPR * BNP * sizeof(float2);
+constexpr size_t OFF_PQ = OFF_SZX + (((size_t)BNP * sizeof(float) + 15) / 16) * 16;
+constexpr size_t RHS_SMEM = OFF_PQ + (size_t)2 * NPQ * CNP * sizeof(float2);
 static_assert(OFF_U01 % 16 == 0 && OFF_U2 % 16 == 0 && OFF_PR % 16 == 0 && OFF_SZX % 16 == 0 && OFF_PQ % 16 == 0,
               "16-byte aligned regions");
 // phase-1 thread roles of fused_rhs: stage-1 strips of the B region, then the velocity strips
@@ -172,12 +177,12 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
   float* const oPs[3] = {I.Ps[par ^ 1][0], I.Ps[par ^ 1][1], I.Ps[par ^ 1][2]};
   float* const ophi = I.phi[par ^ 1];
   float* const phic = I.phic;
-  float2* const sA = reinterpret_cast<float2*>(smr + OFF_A);      // [RA][2][AN]: (phi, Px), (Py, Pz)
-  float2* const sU01 = reinterpret_cast<float2*>(smr + OFF_U01);  // [RU][BN]: (ux, uy)
-  float* const sU2 = reinterpret_cast<float*>(smr + OFF_U2);      // [RU][BN]: uz
-  float2* const sPr = reinterpret_cast<float2*>(smr + OFF_PR);    // [NPR][BN]
-  float* const sSzx = reinterpret_cast<float*>(smr + OFF_SZX);    // [BN]
-  float2* const sQ = reinterpret_cast<float2*>(smr + OFF_PQ);     // [2][NPQ][CN]
+  float2* const sA = reinterpret_cast<float2*>(smr + OFF_A);      // [RA][2][ANP]: (phi, Px), (Py, Pz)
+  float2* const sU01 = reinterpret_cast<float2*>(smr + OFF_U01);  // [RU][BNP]: (ux, uy)
+  float* const sU2 = reinterpret_cast<float*>(smr + OFF_U2);      // [RU][BNP]: uz
+  float2* const sPr = reinterpret_cast<float2*>(smr + OFF_PR);    // [NPR][BNP]
+  float* const sSzx = reinterpret_cast<float*>(smr + OFF_SZX);    // [BNP]
+  float2* const sQ = reinterpret_cast<float2*>(smr + OFF_PQ);     // [2][NPQ][CNP]
   const int tid = threadIdx.x;
   const int niter = (z1 - z0) + 4;
 
@@ -187,42 +192,47 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
   // Offsets within a plane of the elements this thread copies (t = tid + k NT of the A region,
   // tile+2, and of the B region, tile+1), with the periodic wrap: the same for every plane.
   constexpr int KA = (AN + NT - 1) / NT, KB = (BN + NT - 1) / NT;
-  int offA[KA], offB[KB];
+  // (and their shared-memory index in the padded rows)
+  int offA[KA], offB[KB], sidA[KA], sidB[KB];
 #pragma unroll
   for (int k = 0; k < KA; ++k) {
     const int t = tid + k * NT;
     offA[k] = t < AN ? wrapN(y0 - 2 + t / AW, N) * N + wrapN(x0 - 2 + t % AW, N) : 0;
+    sidA[k] = t + t / AW;
   }
 #pragma unroll
   for (int k = 0; k < KB; ++k) {
     const int t = tid + k * NT;
     offB[k] = t < BN ? wrapN(y0 - 1 + t / BW, N) * N + wrapN(x0 - 1 + t % BW, N) : 0;
+    sidB[k] = t + t / BW;
   }
   auto issue = [&](int i) {
     const size_t za = (size_t)wrapN(z0 - 2 + i, N) * NN;
-    float* dst = reinterpret_cast<float*>(sA + (i % RA) * 2 * AN);
+    float* dst = reinterpret_cast<float*>(sA + (i % RA) * 2 * ANP);
 #pragma unroll
     for (int k = 0; k < KA; ++k) {
       const int t = tid + k * NT;
       if (t < AN) {
         const size_t g = za + offA[k];
-        cp_async4(dst + 2 * t, gphi + g);
-        cp_async4(dst + 2 * t + 1, gP[0] + g);
-        cp_async4(dst + 2 * (AN + t), gP[1] + g);
-        cp_async4(dst + 2 * (AN + t) + 1, gP[2] + g);
+        const int d = sidA[k];
+        cp_async4(dst + 2 * d, gphi + g);
+        cp_async4(dst + 2 * d + 1, gP[0] + g);
+        cp_async4(dst + 2 * (ANP + d), gP[1] + g);
+        cp_async4(dst + 2 * (ANP + d) + 1, gP[2] + g);
       }
     }
     const size_t zu = (size_t)wrapN(z0 - 3 + i, N) * NN;
-    float* du = reinterpret_cast<float*>(sU01 + (i % RU) * BN);
-    float* dz = sU2 + (i % RU) * BN;
+    float* du = reinterpret_cast<float*>(sU01 + (i % RU) * BNP);
+    float* dz = sU2 + (i % RU) * BNP;
 #pragma unroll
     for (int k = 0; k < KB; ++k) {
       const int t = tid + k * NT;
       if (t < BN) {
         const size_t g = zu + offB[k];
-        cp_async4(du + 2 * t, gU[0] + g);
-        cp_async4(du + 2 * t + 1, gU[1] + g);
-        cp_async4(dz + t, gU[2] + g);
+        const int d = sidB[k];
+        cp_async4(du + 2 * d, gU[0] + g);
+        cp_async4(du + 2 * d + 1, gU[1] + g);
+        cp_async4(dz + d, gU[2] + g);
       }
     }
     cp_async_commit();
@@ -236,7 +246,7 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
   const bool halfA = tid < NT / 2;
   const int ps = tid & (NT / 2 - 1);
   const int px = ps % TX, py0 = (ps / TX) * 2;
-  const int pbase = py0 * BW + px;  // B index of window row 0 (site 0's row - 1), column px - 1 + 1 - 1
+  const int pbase = py0 * BP + px;  // B index of window row 0 (site 0's row - 1), column px - 1 + 1 - 1
   // z-combinations carried from plane to plane: for a Laplacian, the partial sum of the plane
   // just finished + 1 and that of the plane after it (rL1, rL2); likewise for the divergences.
   // Half A: cv2[0..3] = rL1 [site][pair], cv2[4..7] = rL2, cv1[0..1] = rX1 [site], cv1[2..3] = rX2;
@@ -262,9 +272,9 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
     // ---- phase 1a, stage 1 at plane b = z0 - 3 + i over B (tile+1): the products mu_0, mu_b,
     //      S_ab that phase 2 differentiates, and on the tile the pointwise parts of the update
     if (i >= 2 && tid < NS1) {
-      const float2* a0 = sA + ((i + RA - 2) % RA) * 2 * AN;  // plane b-1
-      const float2* a1 = sA + ((i + RA - 1) % RA) * 2 * AN;  // plane b
-      const float2* a2 = sA + (i % RA) * 2 * AN;             // plane b+1
+      const float2* a0 = sA + ((i + RA - 2) % RA) * 2 * ANP;  // plane b-1
+      const float2* a1 = sA + ((i + RA - 1) % RA) * 2 * ANP;  // plane b
+      const float2* a2 = sA + (i % RA) * 2 * ANP;             // plane b+1
       // strips of the B region: warps take 32 consecutive columns of one strip row (unit-stride
       // shared-memory access); the last BW - 32 columns of every row come after them
       constexpr int NSR = BH / RB, NMAIN = 32 * NSR;
@@ -272,46 +282,46 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
       int bx, by0;
       if (s < NMAIN) { bx = s & 31; by0 = (s >> 5) * RB; }
       else { const int e = s - NMAIN; bx = 32 + e % (BW - 32); by0 = (e / (BW - 32)) * RB; }
-      const int base = by0 * AW + bx;  // A index of row offset -1, column offset -1 of site 0
+      const int base = by0 * AP + bx;  // A index of row offset -1, column offset -1 of site 0
       // pair 0 = (phi, Px), pair 1 = (Py, Pz): D_a (3), L and the centre value of each site
       float2 D0[3][RB], L0[RB], C0[RB], D1[3][RB], L1[RB], C1[RB];
       {
         auto ld = [&](int z, int r, int c) {
           const float2* pl = z == 0 ? a0 : (z == 1 ? a1 : a2);
-          return pl[base + r * AW + c];
+          return pl[base + r * AP + c];
         };
         sep_rows<RB, true, true, true, true, float2>(ld, sk, D0[0], D0[1], D0[2], L0, C0);
       }
       {
         auto ld = [&](int z, int r, int c) {
           const float2* pl = z == 0 ? a0 : (z == 1 ? a1 : a2);
-          return pl[AN + base + r * AW + c];
+          return pl[ANP + base + r * AP + c];
         };
         sep_rows<RB, true, true, true, true, float2>(ld, sk, D1[0], D1[1], D1[2], L1, C1);
       }
-      const float2* ubp = sU01 + (i % RU) * BN;  // u at plane b
-      const float* ubz = sU2 + (i % RU) * BN;
-      float2* pq = sQ + (i & 1) * NPQ * CN;
+      const float2* ubp = sU01 + (i % RU) * BNP;  // u at plane b
+      const float* ubz = sU2 + (i % RU) * BNP;
+      float2* pq = sQ + (i & 1) * NPQ * CNP;
 #pragma unroll
       for (int k = 0; k < RB; ++k) {
-        const int o = (by0 + k) * BW + bx;
+        const int o = (by0 + k) * BP + bx;
         const float ph = C0[k].x, px = C0[k].y, py = C1[k].x, pz = C1[k].y;
         // mu_0 = aPhi 2(phi - 3phi^2 + 2phi^3) - kPhi L phi (:567), mu_b = phi P_b + La^2 L P_b (:571-573)
         const float poly = p.aPhi2 * (ph - 3 * ph * ph + 2 * ph * ph * ph);
         const float2 M0 = vfma(f2(-p.kPhi, p.La2), L0[k], f2(poly, ph * px));
         const float2 M1 = vfma(vsplat(p.La2, float2()), L1[k], vmul(vsplat(ph, float2()), C1[k]));
-        sPr[PM0 * BN + o] = M0;
-        sPr[PM1 * BN + o] = M1;
+        sPr[PM0 * BNP + o] = M0;
+        sPr[PM1 * BNP + o] = M1;
         // S_ab = cA phi D_a P_b - zeta phi P_a P_b (:587-595 and the active stress)
         const float cph = p.cA * ph, zph = p.zeta * ph;
         const float Pa[3] = {px, py, pz};
         float sx[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-          sPr[(PT0 + a) * BN + o] = vfma(vsplat(cph, float2()), D1[a][k], vmul(vsplat(-zph * Pa[a], float2()), C1[k]));
+          sPr[(PT0 + a) * BNP + o] = vfma(vsplat(cph, float2()), D1[a][k], vmul(vsplat(-zph * Pa[a], float2()), C1[k]));
           sx[a] = fmaf(cph, D0[a][k].y, -zph * Pa[a] * px);
         }
-        sPr[PT3 * BN + o] = f2(sx[0], sx[1]);
+        sPr[PT3 * BNP + o] = f2(sx[0], sx[1]);
         sSzx[o] = sx[2];
         const int cx = bx - 1, cy = by0 + k - 1;
         if (cx >= 0 && cx < TX && cy >= 0 && cy < TY) {
@@ -319,7 +329,7 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
           //   u_b:  mu_0 D_b phi;  phi: -u.D phi;
           //   P_b:  -(u + lambda0 P).D P_b - P_b (alpha phi + beta |P|^2 + A |D phi|^2 |P|^2)
           //         - A |P| (D phi . P) D_b phi
-          const int c = cy * TX + cx;
+          const int c = cy * CP + cx;
           const float2 uxy = ubp[o];
           const float vx = uxy.x, vy = uxy.y, vz = ubz[o];
           const float mu0 = M0.x;
@@ -330,16 +340,16 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
           const float kap = p.alpha * ph + P2 * (p.beta + p.A * G2);
           const float m = p.A * sqrtf(P2) * GP;
           const float wx = fmaf(p.lambda0, px, vx), wy = fmaf(p.lambda0, py, vy), wz = fmaf(p.lambda0, pz, vz);
-          pq[0 * CN + c] = f2(mu0 * gx, mu0 * gy);
-          pq[1 * CN + c] = f2(mu0 * gz, -(vx * gx + vy * gy + vz * gz));
+          pq[0 * CNP + c] = f2(mu0 * gx, mu0 * gy);
+          pq[1 * CNP + c] = f2(mu0 * gz, -(vx * gx + vy * gy + vz * gz));
           const float ppx = -(wx * D0[0][k].y + wy * D0[1][k].y + wz * D0[2][k].y) - kap * px - m * gx;
           float2 t = vmul(vsplat(wx, float2()), D1[0][k]);
           t = vfma(vsplat(wy, float2()), D1[1][k], t);
           t = vfma(vsplat(wz, float2()), D1[2][k], t);
           t = vfma(vsplat(kap, float2()), C1[k], t);
           t = vfma(vsplat(m, float2()), f2(gy, gz), t);
-          pq[2 * CN + c] = f2(ppx, -t.x);
-          pq[3 * CN + c] = f2(-t.y, 0.f);
+          pq[2 * CNP + c] = f2(ppx, -t.x);
+          pq[3 * CNP + c] = f2(-t.y, 0.f);
         }
       }
     }
@@ -350,35 +360,35 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
       const int s = tid - NU0;
       const int vx = s & 31, vy0 = (s >> 5) * US;  // tile coordinates of the strip
       const int sl0 = (i + RU - 2) % RU, sl1 = (i + RU - 1) % RU, sl2 = i % RU;  // planes c-1, c, c+1
-      const int base = vy0 * BW + vx;  // B index of row offset -1, column offset -1 of site 0
+      const int base = vy0 * BP + vx;  // B index of row offset -1, column offset -1 of site 0
       float2 Dp[3][US], Lp[US], Cp[US];
       float Dz[3][US], Lz[US], Cz[US];
       {
         auto ld = [&](int z, int r, int c) {
           const int sl = z == 0 ? sl0 : (z == 1 ? sl1 : sl2);
-          return sU01[sl * BN + base + r * BW + c];
+          return sU01[sl * BNP + base + r * BP + c];
         };
         sep_rows<US, true, true, true, true, float2>(ld, sk, Dp[0], Dp[1], Dp[2], Lp, Cp);
       }
       {
         auto ld = [&](int z, int r, int c) {
           const int sl = z == 0 ? sl0 : (z == 1 ? sl1 : sl2);
-          return sU2[sl * BN + base + r * BW + c];
+          return sU2[sl * BNP + base + r * BP + c];
         };
         sep_rows<US, true, true, true, true, float>(ld, sk, Dz[0], Dz[1], Dz[2], Lz, Cz);
       }
-      float2* pq = sQ + ((i + 1) & 1) * NPQ * CN;
+      float2* pq = sQ + ((i + 1) & 1) * NPQ * CNP;
 #pragma unroll
       for (int k = 0; k < US; ++k) {
-        const int c = (vy0 + k) * TX + vx;
+        const int c = (vy0 + k) * CP + vx;
         const float ux = Cp[k].x, uy = Cp[k].y, uz = Cz[k];
         float2 t = vmul(vsplat(-ux, float2()), Dp[0][k]);
         t = vfma(vsplat(-uy, float2()), Dp[1][k], t);
         t = vfma(vsplat(-uz, float2()), Dp[2][k], t);
         t = vfma(vsplat(p.mu, float2()), Lp[k], t);
         const float tz = fmaf(p.mu, Lz[k], -(ux * Dz[0][k] + uy * Dz[1][k] + uz * Dz[2][k]));
-        pq[0 * CN + c] = vadd(pq[0 * CN + c], t);
-        pq[1 * CN + c].x += tz;
+        pq[0 * CNP + c] = vadd(pq[0 * CNP + c], t);
+        pq[1 * CNP + c].x += tz;
       }
     }
     __syncthreads();
@@ -386,20 +396,20 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
     //      b, carried in z; plane c = b - 1 is then complete
     if (i >= 2) {
       const int zc = z0 - 4 + i;
-      const float2* pq = sQ + ((i + 1) & 1) * NPQ * CN;     // plane c: stage 1 + velocity terms
+      const float2* pq = sQ + ((i + 1) & 1) * NPQ * CNP;    // plane c: stage 1 + velocity terms
       const int sl = (i + RU - 1) % RU;                     // u at plane c
-      const float2* ac = sA + ((i + RA - 2) % RA) * 2 * AN;  // phi, P at plane c
+      const float2* ac = sA + ((i + RA - 2) % RA) * 2 * ANP;  // phi, P at plane c
       const float2 four = f2(4.f, 4.f);
       if (halfA) {
         float2 lm[2][2];  // [site]: (L mu_0, L mu_x), (L mu_y, L mu_z)
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
-          const float2* F = sPr + (PM0 + q) * BN + pbase;
+          const float2* F = sPr + (PM0 + q) * BNP + pbase;
           float2 v[4][3];
 #pragma unroll
           for (int r = 0; r < 4; ++r)
 #pragma unroll
-            for (int c = 0; c < 3; ++c) v[r][c] = F[r * BW + c];
+            for (int c = 0; c < 3; ++c) v[r][c] = F[r * BP + c];
 #pragma unroll
           for (int k = 0; k < 2; ++k) {
             const float2 ce = v[k + 1][1];
@@ -415,7 +425,7 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
         // divergence column x: X of S_xx (T3.x), Y of S_yx (T3.y), Z of S_zx
         float dvx[2];
         {
-          const float2* T = sPr + PT3 * BN + pbase;
+          const float2* T = sPr + PT3 * BNP + pbase;
           const float* Zs = sSzx + pbase;
           float2 t[4][3];
           float z[4][3];
@@ -423,8 +433,8 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
           for (int r = 0; r < 4; ++r)
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-              t[r][c] = T[r * BW + c];
-              z[r][c] = Zs[r * BW + c];
+              t[r][c] = T[r * BP + c];
+              z[r][c] = Zs[r * BP + c];
             }
 #pragma unroll
           for (int k = 0; k < 2; ++k) {
@@ -445,12 +455,12 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
         if (i >= 4) {
 #pragma unroll
           for (int k = 0; k < 2; ++k) {
-            const int c = (py0 + k) * TX + px, oa = (py0 + k + 2) * AW + (px + 2), ob = (py0 + k + 1) * BW + (px + 1);
+            const int c = (py0 + k) * CP + px, oa = (py0 + k + 2) * AP + (px + 2), ob = (py0 + k + 1) * BP + (px + 1);
             const size_t g = (size_t)zc * NN + (size_t)(y0 + py0 + k) * N + (x0 + px);
-            const float2 q0 = pq[0 * CN + c], q1 = pq[1 * CN + c], q2 = pq[2 * CN + c], q3 = pq[3 * CN + c];
-            const float2 A0 = ac[oa], A1 = ac[AN + oa];
+            const float2 q0 = pq[0 * CNP + c], q1 = pq[1 * CNP + c], q2 = pq[2 * CNP + c], q3 = pq[3 * CNP + c];
+            const float2 A0 = ac[oa], A1 = ac[ANP + oa];
             // u*_x = u_x + dt d/dt u_x (:480-482)
-            oUs[0][g] = fmaf(p.dt, fmaf(sk.d, dvx[k], q0.x), sU01[sl * BN + ob].x);
+            oUs[0][g] = fmaf(p.dt, fmaf(sk.d, dvx[k], q0.x), sU01[sl * BNP + ob].x);
             // P*_b = P_b + dt (pointwise part + eta L mu_b) (:623-629, :486-488)
             oPs[0][g] = fmaf(p.dt, fmaf(p.eta, lm[k][0].y, q2.x), A0.y);
             const float2 ps2 = vfma(vsplat(p.dt, float2()), vfma(vsplat(p.eta, float2()), lm[k][1], f2(q2.y, q3.x)), A1);
@@ -471,18 +481,18 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
         // Z of T2 = (S_zy, S_zz)
         float2 dv[2];
         {
-          const float2* X = sPr + PT0 * BN + pbase;
-          const float2* Y = sPr + PT1 * BN + pbase;
-          const float2* Z = sPr + PT2 * BN + pbase;
+          const float2* X = sPr + PT0 * BNP + pbase;
+          const float2* Y = sPr + PT1 * BNP + pbase;
+          const float2* Z = sPr + PT2 * BNP + pbase;
           float2 xa[4][2], ya[4][3], za[4][3];
 #pragma unroll
           for (int r = 0; r < 4; ++r) {
-            xa[r][0] = X[r * BW];
-            xa[r][1] = X[r * BW + 2];
+            xa[r][0] = X[r * BP];
+            xa[r][1] = X[r * BP + 2];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-              ya[r][c] = Y[r * BW + c];
-              za[r][c] = Z[r * BW + c];
+              ya[r][c] = Y[r * BP + c];
+              za[r][c] = Z[r * BP + c];
             }
           }
 #pragma unroll
@@ -504,12 +514,12 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
         if (i >= 4) {
 #pragma unroll
           for (int k = 0; k < 2; ++k) {
-            const int c = (py0 + k) * TX + px, ob = (py0 + k + 1) * BW + (px + 1);
+            const int c = (py0 + k) * CP + px, ob = (py0 + k + 1) * BP + (px + 1);
             const size_t g = (size_t)zc * NN + (size_t)(y0 + py0 + k) * N + (x0 + px);
-            const float2 q0 = pq[0 * CN + c], q1 = pq[1 * CN + c];
+            const float2 q0 = pq[0 * CNP + c], q1 = pq[1 * CNP + c];
             // (u*_y, u*_z) = (u_y, u_z) + dt d/dt (u_y, u_z) (:480-482)
             const float2 us = vfma(vsplat(p.dt, float2()), vfma(vsplat(sk.d, float2()), dv[k], f2(q0.y, q1.x)),
-                                   f2(sU01[sl * BN + ob].y, sU2[sl * BN + ob]));
+                                   f2(sU01[sl * BNP + ob].y, sU2[sl * BNP + ob]));
             oUs[1][g] = us.x;
             oUs[2][g] = us.y;
           }
@@ -546,7 +556,11 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 
-__global__ void __launch_bounds__(NTC, 2) k_fused_div(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc) {
+// fused_div: 2-site strips (a 4 x 3 window of each staged field serves both sites), u* and P*
+// as a packed pair.
+constexpr int NTV = TX * TY / 2;  // 256 threads
+
+__global__ void __launch_bounds__(NTV, 3) k_fused_div(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc) {
   extern __shared__ __align__(16) float sm[];
   const int N = insts[0].N;
   const InstDev<float>& I = insts[blockIdx.z / nchunk];
@@ -571,7 +585,7 @@ __global__ void __launch_bounds__(NTC, 2) k_fused_div(const InstDev<float>* __re
     const int zz = wrapN(zu, N);
     float* dst = sm + (i % DR) * 6 * SPL;
     constexpr int CR = SW / 4;  // chunks per row
-    for (int t = tid; t < SH * CR; t += NTC) {
+    for (int t = tid; t < SH * CR; t += NTV) {
       const int ry = t / CR, rc = t - ry * CR;
       const int gx = x0 - 4 + 4 * rc, gy = y0 - 1 + ry;
       const bool stale = stale_q2 && (zw || gx < 0 || gx >= N || gy < 0 || gy >= N);
@@ -581,37 +595,48 @@ __global__ void __launch_bounds__(NTC, 2) k_fused_div(const InstDev<float>* __re
     }
     cp_async_commit();
   };
-  const int qx = tid % TX, qy = tid / TX;
-  const size_t gc = (size_t)(y0 + qy) * N + (x0 + qx);
-  // the divergence D_x v_x + D_y v_y + D_z v_z of v = u*, P* (getStream mode 0, :664-670), each
+  const int qx = tid % TX, qy0 = (tid / TX) * 2;
+  const size_t gc0 = (size_t)(y0 + qy0) * N + (x0 + qx);
+  const int wbase = qy0 * SW + (qx + 3);  // staged index of window row 0 (site 0's row - 1), column x - 1
+  // the divergence D_x v_x + D_y v_y + D_z v_z of v = (u*, P*) (getStream mode 0, :664-670), each
   // D = d/36 delta s s: a plane adds Q = delta_x s_y v_x + s_x delta_y v_y with weight s_z =
   // (1, 4, 1) and Z = s_x s_y v_z with weight delta_z = (-1, 0, 1) over planes c-1, c, c+1
-  float rD1[2] = {0.f, 0.f}, rD2[2] = {0.f, 0.f};
+  float2 rD1[2] = {f2(0.f, 0.f), f2(0.f, 0.f)}, rD2[2] = {f2(0.f, 0.f), f2(0.f, 0.f)};  // [site]
+  const float2 four = f2(4.f, 4.f);
 #pragma unroll
   for (int k = 0; k < DR - 1; ++k) issue(k);
   for (int i = 0; i < niter; ++i) {
     cp_async_wait_ring();
     __syncthreads();
     issue(i + DR - 1);  // into the slot read at iteration i - 1
-    const float* s = sm + (i % DR) * 6 * SPL + (qy + 1) * SW + (qx + 4);
-    float dv[2];
+    const float* s = sm + (i % DR) * 6 * SPL + wbase;
+    auto w = [&](int comp, int r, int c) { return f2(s[comp * SPL + r * SW + c], s[(3 + comp) * SPL + r * SW + c]); };
+    float2 X[4][2], Y[4][3], Z[4][3];
 #pragma unroll
-    for (int f = 0; f < 2; ++f) {
-      const float* X = s + (3 * f + 0) * SPL;
-      const float* Y = s + (3 * f + 1) * SPL;
-      const float* Z = s + (3 * f + 2) * SPL;
-      const float xr = fmaf(4.f, X[1], X[-SW + 1] + X[SW + 1]) - fmaf(4.f, X[-1], X[-SW - 1] + X[SW - 1]);
-      const float yr = fmaf(4.f, Y[SW] - Y[-SW], (Y[SW - 1] - Y[-SW - 1]) + (Y[SW + 1] - Y[-SW + 1]));
-      const float t0 = fmaf(4.f, Z[-1], Z[-SW - 1] + Z[SW - 1]);
-      const float t1 = fmaf(4.f, Z[0], Z[-SW] + Z[SW]);
-      const float t2 = fmaf(4.f, Z[1], Z[-SW + 1] + Z[SW + 1]);
-      const float zr = fmaf(4.f, t1, t0 + t2);
-      const float Q = xr + yr;
-      dv[f] = rD1[f] + Q + zr;
-      rD1[f] = fmaf(4.f, Q, rD2[f]);
-      rD2[f] = Q - zr;
+    for (int r = 0; r < 4; ++r) {
+      X[r][0] = w(0, r, 0);
+      X[r][1] = w(0, r, 2);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        Y[r][c] = w(1, r, c);
+        Z[r][c] = w(2, r, c);
+      }
     }
-    if (i >= 2) oW[(size_t)(z0 - 2 + i) * NN + gc] = make_float2(kd * dv[0], kd * dv[1]);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const float2 xr = vsub(vfma(four, X[k + 1][1], vadd(X[k][1], X[k + 2][1])),
+                             vfma(four, X[k + 1][0], vadd(X[k][0], X[k + 2][0])));
+      const float2 yr = vfma(four, vsub(Y[k + 2][1], Y[k][1]), vadd(vsub(Y[k + 2][0], Y[k][0]), vsub(Y[k + 2][2], Y[k][2])));
+      const float2 t0 = vfma(four, Z[k + 1][0], vadd(Z[k][0], Z[k + 2][0]));
+      const float2 t1 = vfma(four, Z[k + 1][1], vadd(Z[k][1], Z[k + 2][1]));
+      const float2 t2 = vfma(four, Z[k + 1][2], vadd(Z[k][2], Z[k + 2][2]));
+      const float2 zr = vfma(four, t1, vadd(t0, t2));
+      const float2 Q = vadd(xr, yr);
+      const float2 dv = vadd(vadd(rD1[k], Q), zr);
+      rD1[k] = vfma(four, Q, rD2[k]);
+      rD2[k] = vsub(Q, zr);
+      if (i >= 2) oW[(size_t)(z0 - 2 + i) * NN + gc0 + (size_t)k * N] = vmul(vsplat(kd, float2()), dv);
+    }
   }
 }
 
@@ -741,7 +766,7 @@ void launch_fused_rhs(const Group<float>& g, int par, cudaStream_t st) {
 void launch_fused_div(const Group<float>& g, int par, cudaStream_t st) {
   int nchunk;
   dim3 grid = grid_for(g, g.zc[1], nchunk);
-  k_fused_div<<<grid, NTC, DIV_SMEM, st>>>(g.d_inst, par, nchunk, g.zc[1]);
+  k_fused_div<<<grid, NTV, DIV_SMEM, st>>>(g.d_inst, par, nchunk, g.zc[1]);
   check(cudaGetLastError(), "fused_div launch");
 }
 
