@@ -61,9 +61,25 @@ std::vector<int> radix_plan(int N) {
 
 // Kernel classes reported by ttsh_profile_kernels.
 enum KClass { K_STAGE1, K_STAGE2, K_DIV, K_FFT0, K_FFT1, K_FFT2, K_FFT3, K_FFT4, K_CORRECT, K_FUSED_RHS,
-              K_FUSED_DIV, K_FUSED_CORRECT, K_NCLASS };
+              K_FUSED_DIV, K_FUSED_CORRECT, K_FFT_XY, K_FFT_YX, K_NCLASS };
 const char* kNames[K_NCLASS] = {"stage1", "stage2", "div", "fft_x_fwd", "fft_y_fwd", "fft_z_poisson", "fft_y_inv",
-                                "fft_x_inv", "correct", "fused_rhs", "fused_div", "fused_correct"};
+                                "fft_x_inv", "correct", "fused_rhs", "fused_div", "fused_correct",
+                                "fft_xy_fwd", "fft_yx_inv"};
+
+// The Poisson solve of a group: x+y per plane, z, y+x per plane (fft_kind 2 with a register
+// kernel for the size), else one launch per axis pass. `run(class, launch)` wraps each launch.
+template <class T, class R>
+void enqueue_fft(const Group<T>& g, cudaStream_t st, R&& run) {
+  if (g.fft_kind == 2 && fftreg_has<T>(g.N)) {
+    run(K_FFT_XY, [&] { fftreg_plane_launch<T>(g, 0, st); });
+    run(K_FFT2, [&] { launch_fft_pass<T>(g, 2, st); });
+    run(K_FFT_YX, [&] { fftreg_plane_launch<T>(g, 1, st); });
+  } else {
+    for (int pass = 0; pass < 5; ++pass) run(K_FFT0 + pass, [&] { launch_fft_pass<T>(g, pass, st); });
+  }
+}
+template <class T>
+int fft_launches(const Group<T>& g) { return (g.fft_kind == 2 && fftreg_has<T>(g.N)) ? 3 : 5; }
 
 struct Prof {
   cudaStream_t st;
@@ -114,7 +130,7 @@ struct Engine {
         run(K_STAGE2, [&] { launch_stage2<T>(g, par, st); });
         run(K_DIV, [&] { launch_div<T>(g, par, st); });
       }
-      for (int pass = 0; pass < 5; ++pass) run(K_FFT0 + pass, [&] { launch_fft_pass<T>(g, pass, st); });
+      enqueue_fft(g, st, run);
       if (fused) run(K_FUSED_CORRECT, [&] { launch_fused_correct_t(g, par, st); });
       else run(K_CORRECT, [&] { launch_correct<T>(g, par, st); });
     }
@@ -122,7 +138,11 @@ struct Engine {
   void launch_fused_rhs_t(const Group<T>& g, int par, cudaStream_t st);
   void launch_fused_div_t(const Group<T>& g, int par, cudaStream_t st);
   void launch_fused_correct_t(const Group<T>& g, int par, cudaStream_t st);
-  int launches(bool fused) const { return (int)groups.size() * (fused ? 8 : 9); }
+  int launches(bool fused) const {
+    int n = 0;
+    for (const auto& g : groups) n += (fused ? 3 : 4) + fft_launches(g);
+    return n;
+  }
 };
 
 template <>
@@ -320,8 +340,10 @@ void build_engine(ttsh_sim* s, Engine<T>& E) {
     for (size_t k = 0; k < E.members[g].size(); ++k) E.h[E.members[g][k]].red = red + k * per;
     Group<T> G{};
     G.red = red;
-    const char* fk = std::getenv("TTSH_FFT");  // "stockham": shared-memory Stockham passes only
-    G.fft_kind = (fk && std::string(fk) == "stockham") ? 1 : 0;
+    // TTSH_FFT="stockham": shared-memory Stockham passes only; "separate": register passes, one
+    // launch per axis; otherwise register kernels with x and y of a plane in one launch
+    const char* fk = std::getenv("TTSH_FFT");
+    G.fft_kind = (fk && std::string(fk) == "stockham") ? 1 : ((fk && std::string(fk) == "separate") ? 0 : 2);
     G.n = (int)E.members[g].size();
     G.N = s->inst[E.members[g][0]].N;
     std::vector<InstDev<T>> arr;
@@ -492,7 +514,7 @@ void get_tuning(const ttsh_sim* s, const Engine<T>& E, size_t gi, ttsh_tuning* t
 template <class T>
 std::string check_tuning(const ttsh_sim* s, const Group<T>& G, const ttsh_tuning& t) {
   if (t.N != G.N || t.n != G.n) return "tuning: N or group size differs from the group";
-  if (t.fft_kind != 0 && t.fft_kind != 1) return "tuning: fft_kind must be 0 or 1";
+  if (t.fft_kind < 0 || t.fft_kind > 2) return "tuning: fft_kind must be 0, 1 or 2";
   if (t.fft_lb != 0) {
     const std::vector<int> c = fft_lb_candidates<T>(G.N);
     if (std::find(c.begin(), c.end(), t.fft_lb) == c.end()) return "tuning: unsupported Stockham lines per CTA";
@@ -580,12 +602,15 @@ void tune_group(ttsh_sim* s, Engine<T>& E, size_t gi, ttsh_tuning* out) {
       else launch_div<T>(G, par, st);
     };
     auto fft = [&]() {
-      for (int p = 0; p < 5; ++p) launch_fft_pass<T>(G, p, st);
+      enqueue_fft(G, st, [](int, auto&& f) { f(); });
     };
     struct Cand { int kind, lb; std::vector<int> radix; };
     std::vector<Cand> cands;
     const std::vector<std::vector<int>> orders = radix_orders(G.N);
-    if (fftreg_has<T>(G.N)) cands.push_back({0, 0, orders[0]});
+    if (fftreg_has<T>(G.N)) {
+      cands.push_back({2, 0, orders[0]});
+      cands.push_back({0, 0, orders[0]});
+    }
     for (int lb : fft_lb_candidates<T>(G.N))
       for (const auto& o : orders) cands.push_back({1, lb, o});
     double best = 1e30;

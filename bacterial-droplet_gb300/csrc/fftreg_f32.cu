@@ -5,7 +5,11 @@ namespace ttsh {
 
 template <>
 bool fftreg_launch<float>(const Group<float>& g, int pass, cudaStream_t st) {
-  return g.fft_kind == 0 && fftreg::reg_launch<float>(g, pass, st);
+  return g.fft_kind != 1 && fftreg::reg_launch<float>(g, pass, st);
+}
+template <>
+bool fftreg_plane_launch<float>(const Group<float>& g, int dir, cudaStream_t st) {
+  return g.fft_kind == 2 && fftreg::reg_plane_launch<float>(g, dir, st);
 }
 template <>
 bool fftreg_has<float>(int N) {

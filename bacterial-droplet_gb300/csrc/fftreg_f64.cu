@@ -5,7 +5,11 @@ namespace ttsh {
 
 template <>
 bool fftreg_launch<double>(const Group<double>& g, int pass, cudaStream_t st) {
-  return g.fft_kind == 0 && fftreg::reg_launch<double>(g, pass, st);
+  return g.fft_kind != 1 && fftreg::reg_launch<double>(g, pass, st);
+}
+template <>
+bool fftreg_plane_launch<double>(const Group<double>& g, int dir, cudaStream_t st) {
+  return g.fft_kind == 2 && fftreg::reg_plane_launch<double>(g, dir, st);
 }
 template <>
 bool fftreg_has<double>(int N) {

@@ -24,17 +24,15 @@ constexpr size_t smem_bytes(int axis) {
 }
 
 // PASS: 0 forward x, 1 forward y, 2 forward z + Poisson multiplier + inverse z, 3 inverse y,
-// 4 inverse x scaled by 1/N^3.
+// 4 inverse x scaled by 1/N^3. One call transforms line group g of the pass (LB lines) with the
+// CTA's threads; S is the CTA's shared memory.
 template <class T, int N1, int N2, int PASS>
-__global__ void __launch_bounds__(lines_per_cta<N1 * N2>() * N2, (sizeof(T) == 4 && N1 * N2 >= 256 && PASS == 2) ? 3 : 1) k_fftr(const InstDev<T>* __restrict__ insts) {
+__device__ __forceinline__ void fft_lines(const InstDev<T>& I, int g, typename CxT<T>::type* S) {
   typedef typename CxT<T>::type C;
   constexpr int N = N1 * N2;
   constexpr int LB = lines_per_cta<N>();
   constexpr int OW = N1 / N2;  // k1 rows owned by each thread in the second step
   constexpr int axis = (PASS == 0 || PASS == 4) ? 0 : ((PASS == 1 || PASS == 3) ? 1 : 2);
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  C* S = reinterpret_cast<C*>(smem_raw);
-  const InstDev<T>& I = insts[blockIdx.y];
   C* __restrict__ W = I.W;
   const C* tab = I.tw;
   const size_t NN = (size_t)N * N;
@@ -44,7 +42,6 @@ __global__ void __launch_bounds__(lines_per_cta<N1 * N2>() * N2, (sizeof(T) == 4
   size_t base, stride;
   int xl = 0, yl = 0;
   {
-    const int g = blockIdx.x;
     if (axis == 0) {
       base = ((size_t)g * LB + l) * N;
       stride = 1;
@@ -124,6 +121,56 @@ __global__ void __launch_bounds__(lines_per_cta<N1 * N2>() * N2, (sizeof(T) == 4
 }
 
 template <class T, int N1, int N2, int PASS>
+__global__ void __launch_bounds__(lines_per_cta<N1 * N2>() * N2, (sizeof(T) == 4 && N1 * N2 >= 256 && PASS == 2) ? 3 : 1) k_fftr(const InstDev<T>* __restrict__ insts) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  fft_lines<T, N1, N2, PASS>(insts[blockIdx.y], blockIdx.x, reinterpret_cast<typename CxT<T>::type*>(smem_raw));
+}
+
+// Both in-plane axes of the z-planes, one plane per thread-block cluster of PC CTAs: DIR 0
+// forward x then forward y, DIR 1 inverse y then inverse x (scaled). Each CTA of the cluster
+// takes every PC-th line group of the first axis, the cluster barrier (release / acquire at
+// cluster scope) makes the whole plane's results visible to all of its CTAs, then each takes
+// every PC-th line group of the second axis. The plane's intermediate (N^2 complex values) is
+// written and read back a few microseconds apart, so it stays in L2 instead of making an HBM
+// round trip between two separate passes over the whole volume.
+template <int N>
+constexpr int plane_parts() {
+  constexpr int NG = N / lines_per_cta<N>();
+  return NG % 4 == 0 ? 4 : (NG % 2 == 0 ? 2 : (NG % 3 == 0 ? 3 : 1));
+}
+
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+  asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+template <class T, int N1, int N2, int DIR>
+__global__ void __cluster_dims__(plane_parts<N1 * N2>(), 1, 1) __launch_bounds__(lines_per_cta<N1 * N2>() * N2)
+    k_fftr_plane(const InstDev<T>* __restrict__ insts) {
+  typedef typename CxT<T>::type C;
+  constexpr int N = N1 * N2;
+  constexpr int NG = N / lines_per_cta<N>();  // line groups of one axis within a plane
+  constexpr int PC = plane_parts<N>();
+  static_assert(NG % PC == 0, "the cluster splits a plane's line groups evenly");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* S = reinterpret_cast<C*>(smem_raw);
+  const InstDev<T>& I = insts[blockIdx.y];
+  const int z = blockIdx.x / PC, part = blockIdx.x % PC;
+  // x lines of plane z are the row groups z*NG .. z*NG + NG - 1 of pass 0 / 4; its y lines the
+  // groups z*NG .. of pass 1 / 3 (outer index z). __syncthreads between groups: the next group
+  // reuses S.
+  if constexpr (DIR == 0) {
+    for (int gg = part; gg < NG; gg += PC) { fft_lines<T, N1, N2, 0>(I, z * NG + gg, S); __syncthreads(); }
+    cluster_sync_all();
+    for (int gg = part; gg < NG; gg += PC) { fft_lines<T, N1, N2, 1>(I, z * NG + gg, S); __syncthreads(); }
+  } else {
+    for (int gg = part; gg < NG; gg += PC) { fft_lines<T, N1, N2, 3>(I, z * NG + gg, S); __syncthreads(); }
+    cluster_sync_all();
+    for (int gg = part; gg < NG; gg += PC) { fft_lines<T, N1, N2, 4>(I, z * NG + gg, S); __syncthreads(); }
+  }
+}
+
+template <class T, int N1, int N2, int PASS>
 void launch_pass(const Group<T>& g, cudaStream_t st) {
   constexpr int N = N1 * N2;
   constexpr int LB = lines_per_cta<N>();
@@ -132,6 +179,17 @@ void launch_pass(const Group<T>& g, cudaStream_t st) {
   k_fftr<T, N1, N2, PASS><<<dim3(nblk, g.n), LB * N2, smem_bytes<T, N1, N2>(axis), st>>>(g.d_inst);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) throw std::runtime_error(std::string("fft (register) launch: ") + cudaGetErrorString(e));
+}
+
+template <class T, int N1, int N2, int DIR>
+void launch_plane(const Group<T>& g, cudaStream_t st) {
+  constexpr int N = N1 * N2;
+  constexpr int LB = lines_per_cta<N>();
+  constexpr size_t smem = smem_bytes<T, N1, N2>(0) > smem_bytes<T, N1, N2>(1) ? smem_bytes<T, N1, N2>(0)
+                                                                                : smem_bytes<T, N1, N2>(1);
+  k_fftr_plane<T, N1, N2, DIR><<<dim3(N * plane_parts<N>(), g.n), LB * N2, smem, st>>>(g.d_inst);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) throw std::runtime_error(std::string("fft (register, plane) launch: ") + cudaGetErrorString(e));
 }
 
 template <class T, int N1, int N2>
@@ -145,6 +203,9 @@ void prepare_size() {
   set((const void*)k_fftr<T, N1, N2, 2>, smem_bytes<T, N1, N2>(2));
   set((const void*)k_fftr<T, N1, N2, 3>, smem_bytes<T, N1, N2>(1));
   set((const void*)k_fftr<T, N1, N2, 4>, smem_bytes<T, N1, N2>(0));
+  const size_t sp = smem_bytes<T, N1, N2>(0) > smem_bytes<T, N1, N2>(1) ? smem_bytes<T, N1, N2>(0) : smem_bytes<T, N1, N2>(1);
+  set((const void*)k_fftr_plane<T, N1, N2, 0>, sp);
+  set((const void*)k_fftr_plane<T, N1, N2, 1>, sp);
 }
 
 template <class T, int N1, int N2>
@@ -191,6 +252,16 @@ void reg_prepare(int N) {
     TTSH_FFTREG_SIZES(X)
 #undef X
     default: break;
+  }
+}
+
+template <class T>
+bool reg_plane_launch(const Group<T>& g, int dir, cudaStream_t st) {
+  switch (g.N) {
+#define X(n, a, b) case n: if (dir == 0) launch_plane<T, a, b, 0>(g, st); else launch_plane<T, a, b, 1>(g, st); return true;
+    TTSH_FFTREG_SIZES(X)
+#undef X
+    default: return false;
   }
 }
 

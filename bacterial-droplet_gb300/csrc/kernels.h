@@ -14,7 +14,8 @@ struct Group {
   InstDev<T>* d_inst;  // device array [n]
   int n;               // instances in the group
   int N;
-  int fft_kind = 0;    // 0: register-resident FFT kernels where the size has them; 1: Stockham only
+  int fft_kind = 0;    // register-resident FFT kernels where the size has them: 0 one launch per
+                       // axis pass, 2 x and y of a plane in one launch; 1: Stockham only
   int fft_lb = 0;      // Stockham lines per CTA (0: the largest power of two that fits)
   int zc[3] = {64, 64, 64};  // z-planes per CTA of fused_rhs, fused_div, fused_correct
   double tuned_ms[4] = {0, 0, 0, 0};  // the tuner's timings of this configuration (host record)
@@ -43,6 +44,9 @@ template <class T> int fft_lines(const Group<T>& g);
 template <class T> bool fftreg_launch(const Group<T>& g, int pass, cudaStream_t st);
 template <class T> void fftreg_prepare(int N);
 template <class T> bool fftreg_has(int N);
+// Forward x + y (dir 0) or inverse y + x (dir 1) of every z-plane, one CTA per plane (fft_kind 2):
+// false when the group does not use it.
+template <class T> bool fftreg_plane_launch(const Group<T>& g, int dir, cudaStream_t st);
 
 // Fused FP32 form (fused.cu): rhs (u*, P*, phi'), div (packed Poisson source), correct (u, P).
 void launch_fused_rhs(const Group<float>& g, int par, cudaStream_t st);

@@ -56,6 +56,7 @@ KERNEL_WORDS = {
     "fused_correct": 14,    # reads u*, P* (6) and the packed pressure (2); writes u, P (6)
     "stage1": 17, "stage2": 27, "div": 8, "correct": 14,  # plain form
     "fft_x_fwd": 4, "fft_y_fwd": 4, "fft_z_poisson": 4, "fft_y_inv": 4, "fft_x_inv": 4,
+    "fft_xy_fwd": 4, "fft_yx_inv": 4,  # x and y of a plane in one launch: W read and written once
 }
 
 # DRAM bytes per site of the dominant FP32 kernels, dram__bytes_read.sum + dram__bytes_write.sum
@@ -365,8 +366,8 @@ def main():
                 "l2": "inputs larger than L2 (%.1f GB of fields per GPU)" % (sites * 22 * wbytes / 1e9),
                 "parallelism": "replicas" if world > 1 else "1 GPU",
                 "tuning": "default" if tuning is None else [
-                    "N=%d x%d: fft %s, zc %s" % (t["N"], t["n"], "register" if t["fft_kind"] == 0 else
-                                                 "stockham lb=%d radix=%s" % (t["fft_lb"], t["radix"]), t["zc"])
+                    "N=%d x%d: fft %s, zc %s" % (t["N"], t["n"], {0: "register per axis", 2: "register x+y per plane"}.get(
+                        t["fft_kind"], "stockham lb=%d radix=%s" % (t["fft_lb"], t["radix"])), t["zc"])
                     for t in tuning]},
             "hbm_pct_of_step": 100 * hbm_frac,
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,

@@ -206,14 +206,16 @@ int ttsh_struct_size(int which);
 /* Autotuner — no counterpart in the reference (whose tile shapes are fixed by its launch
  * configuration, TTSH3D.cu:224-235, and whose FFT plan is cuFFT's, :1123). The choices are made
  * per group of droplets of equal N (one launch per kernel per group):
- *   the FFT: register-resident passes (where the size has them) or the shared-memory Stockham
- *   passes, with their lines per CTA and the order of the radix plan;
+ *   the FFT: register-resident kernels (where the size has them; per axis, or x and y of a plane
+ *   in one launch) or the shared-memory Stockham passes, with their lines per CTA and the order
+ *   of the radix plan;
  *   the fused FP32 kernels: the z-extent of a CTA's tile (z-planes per CTA) of each of the three.
  * None of them changes results except the FFT choice (rounding order only). */
 typedef struct {
   int N;           /* droplet size of the group */
   int n;           /* droplets in the group */
-  int fft_kind;    /* 0 register-resident passes where the size has them, 1 Stockham */
+  int fft_kind;    /* register-resident kernels where the size has them: 0 one launch per axis
+                      pass, 2 x and y of each plane in one launch; 1 Stockham */
   int fft_lb;      /* Stockham lines per CTA; 0 = the largest that fits */
   int nstages;     /* Stockham radix plan: radix[0..nstages-1], each 2, 3, 4 or 5, product N */
   int radix[16];

@@ -147,16 +147,41 @@ def test_reference_k2_is_not_solenoidal_fp64():
 
 @pytest.mark.parametrize("N", [16, 32, 48])
 def test_fft_kernels_agree(oracle_mod, N, monkeypatch):
-    """The register-resident FFT passes and the shared-memory Stockham passes both match the oracle."""
+    """The register-resident FFT kernels (one launch per axis pass, or x and y of a plane in one
+    launch) and the shared-memory Stockham passes all match the oracle; the two register forms
+    run the same arithmetic, so they agree bit for bit."""
     st = random_state(N, seed=N + 11)
     o = run_oracle(oracle_mod, st, 3, 0, 1, 0.01)
-    monkeypatch.setenv("TTSH_FFT", "stockham")
-    a = run_gpu(st, 3, 64, 0, 1, 0.01)
-    monkeypatch.delenv("TTSH_FFT")
-    b = run_gpu(st, 3, 64, 0, 1, 0.01)
-    for g in (a, b):
+    runs = {}
+    for kind in ("stockham", "separate", None):
+        if kind is None:
+            monkeypatch.delenv("TTSH_FFT", raising=False)
+        else:
+            monkeypatch.setenv("TTSH_FFT", kind)
+        runs[kind] = run_gpu(st, 3, 64, 0, 1, 0.01)
+    monkeypatch.delenv("TTSH_FFT", raising=False)
+    for g in runs.values():
         errs = field_errors(g, o)
         assert max(errs.values()) <= FP64_TOL, errs
+    for k in FIELDS:
+        assert np.array_equal(runs["separate"][k], runs[None][k]), k
+
+
+@pytest.mark.parametrize("N", [64, 256])
+def test_plane_fft_matches_separate_passes_fp32(N, monkeypatch):
+    """FP32 fused form: x and y of each plane in one launch equals one launch per axis pass."""
+    import ttsh
+    st = random_state(N, seed=N + 5)
+    runs = {}
+    for kind in ("separate", None):
+        if kind is None:
+            monkeypatch.delenv("TTSH_FFT", raising=False)
+        else:
+            monkeypatch.setenv("TTSH_FFT", kind)
+        runs[kind] = run_gpu(st, 2, 32, 0, 1, 0.02)
+    monkeypatch.delenv("TTSH_FFT", raising=False)
+    for k in FIELDS:
+        assert np.array_equal(runs["separate"][k], runs[None][k]), k
 
 
 def test_reduce_all_matches_single_reduce():

@@ -73,7 +73,7 @@ def test_set_tuning_rejects_unsupported():
     import ttsh
     with make(ttsh, (64,), 32) as a:
         good = a.tuning()[0]
-        for bad in ({"radix": [4, 4, 2]}, {"radix": [8, 8]}, {"fft_lb": 3}, {"fft_kind": 2}, {"zc": [0, 64, 64]},
+        for bad in ({"radix": [4, 4, 2]}, {"radix": [8, 8]}, {"fft_lb": 3}, {"fft_kind": 3}, {"zc": [0, 64, 64]},
                     {"N": 32}):
             cfg = dict(good, **bad)
             with pytest.raises(ttsh.TTSHError) as e:
