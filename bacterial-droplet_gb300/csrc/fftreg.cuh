@@ -113,7 +113,8 @@ __device__ __forceinline__ float2 poisson_mul(float2 v, const InstDev<float>& I,
     k2 = Kx * Kx + Ky * Ky + Kz * Kz;
     if (k2 < 1e-8f / (I.ph.h * I.ph.h)) return make_float2(0.f, 0.f);
   }
-  const float f = -1.f / k2;
+  // the correctly rounded reciprocal: the value of -1.f / k2 without a full division routine
+  const float f = -__frcp_rn(k2);
   return make_float2(v.x * f, v.y * f);
 }
 

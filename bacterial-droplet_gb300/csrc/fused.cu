@@ -541,8 +541,10 @@ constexpr int SW = TX + 8;              // fused_div row, floats x0 - 4 .. x0 + 
 constexpr int SPL = SW * SH;            // floats per staged plane of one field
 constexpr int CW = TX + 4;              // fused_correct row, float2 x0 - 2 .. x0 + TX + 1
 constexpr int CPL = CW * SH;            // float2 per staged plane
-constexpr int DR = 4;                   // ring slots of fused_div / fused_correct
-constexpr size_t DIV_SMEM = DR * 6 * SPL * sizeof(float);
+constexpr int DR = 4;                   // ring slots of fused_correct
+// fused_div: a taller tile (TX x TYD) and a 3-slot ring (2 planes in flight)
+constexpr int TYD = 32, SHD = TYD + 2, SPLD = SW * SHD, DRD = 3;
+constexpr size_t DIV_SMEM = DRD * 6 * SPLD * sizeof(float);
 constexpr size_t COR_SLOT = CPL * sizeof(float2) + 6 * CN * sizeof(float);  // p_v, p_p on B; u*, P* on C
 constexpr size_t COR_SMEM = DR * COR_SLOT;
 
@@ -556,15 +558,19 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 
-// fused_div: 2-site strips (a 4 x 3 window of each staged field serves both sites), u* and P*
-// as a packed pair.
-constexpr int NTV = TX * TY / 2;  // 256 threads
+// fused_div: 4-site strips of a 32 x 32 tile (a 6 x 3 window of each staged field serves the
+// four sites), u* and P* as a packed pair.
+constexpr int USD = 4;                   // sites per strip
+constexpr int NTV = TX * TYD / USD;      // 256 threads
+__device__ __forceinline__ void cp_async_wait_div() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(DRD - 2) : "memory");
+}
 
-__global__ void __launch_bounds__(NTV, 3) k_fused_div(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc) {
+__global__ void __launch_bounds__(NTV, 2) k_fused_div(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc) {
   extern __shared__ __align__(16) float sm[];
   const int N = insts[0].N;
   const InstDev<float>& I = insts[blockIdx.z / nchunk];
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TYD;
   const int z0 = (blockIdx.z % nchunk) * zc, z1 = min(z0 + zc, N);
   const size_t NN = (size_t)N * N;
   const float* cur[6] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2],
@@ -575,7 +581,7 @@ __global__ void __launch_bounds__(NTV, 3) k_fused_div(const InstDev<float>* __re
   const float kd = I.ph.c2h * (1.f / 36.f) * I.ph.inv_dt;  // d/36 of the 27-point D, and 1/dt
   const int tid = threadIdx.x;
   const int niter = (z1 - z0) + 2;
-  // issue(i): plane z0 - 1 + i into slot i % DR (an empty group past the last plane, so that
+  // issue(i): plane z0 - 1 + i into slot i % DRD (an empty group past the last plane, so that
   // every iteration commits one). Chunks outside the domain come from the previous step's u*, P*
   // when the stale-halo quirk is on (the chunk grid is aligned with 0 and N).
   auto issue = [&](int i) {
@@ -583,54 +589,49 @@ __global__ void __launch_bounds__(NTV, 3) k_fused_div(const InstDev<float>* __re
     const int zu = z0 - 1 + i;
     const bool zw = zu < 0 || zu >= N;
     const int zz = wrapN(zu, N);
-    float* dst = sm + (i % DR) * 6 * SPL;
+    float* dst = sm + (i % DRD) * 6 * SPLD;
     constexpr int CR = SW / 4;  // chunks per row
-    for (int t = tid; t < SH * CR; t += NTV) {
+    for (int t = tid; t < SHD * CR; t += NTV) {
       const int ry = t / CR, rc = t - ry * CR;
       const int gx = x0 - 4 + 4 * rc, gy = y0 - 1 + ry;
       const bool stale = stale_q2 && (zw || gx < 0 || gx >= N || gy < 0 || gy >= N);
       const size_t g = (size_t)zz * NN + (size_t)wrapN(gy, N) * N + wrapN(gx, N);
 #pragma unroll
-      for (int f = 0; f < 6; ++f) cp_async16(dst + f * SPL + ry * SW + 4 * rc, (stale ? old[f] : cur[f]) + g);
+      for (int f = 0; f < 6; ++f) cp_async16(dst + f * SPLD + ry * SW + 4 * rc, (stale ? old[f] : cur[f]) + g);
     }
     cp_async_commit();
   };
-  const int qx = tid % TX, qy0 = (tid / TX) * 2;
+  const int qx = tid % TX, qy0 = (tid / TX) * USD;
   const size_t gc0 = (size_t)(y0 + qy0) * N + (x0 + qx);
   const int wbase = qy0 * SW + (qx + 3);  // staged index of window row 0 (site 0's row - 1), column x - 1
   // the divergence D_x v_x + D_y v_y + D_z v_z of v = (u*, P*) (getStream mode 0, :664-670), each
   // D = d/36 delta s s: a plane adds Q = delta_x s_y v_x + s_x delta_y v_y with weight s_z =
   // (1, 4, 1) and Z = s_x s_y v_z with weight delta_z = (-1, 0, 1) over planes c-1, c, c+1
-  float2 rD1[2] = {f2(0.f, 0.f), f2(0.f, 0.f)}, rD2[2] = {f2(0.f, 0.f), f2(0.f, 0.f)};  // [site]
+  float2 rD1[USD], rD2[USD];  // [site]
+#pragma unroll
+  for (int k = 0; k < USD; ++k) rD1[k] = rD2[k] = f2(0.f, 0.f);
   const float2 four = f2(4.f, 4.f);
 #pragma unroll
-  for (int k = 0; k < DR - 1; ++k) issue(k);
+  for (int k = 0; k < DRD - 1; ++k) issue(k);
   for (int i = 0; i < niter; ++i) {
-    cp_async_wait_ring();
+    cp_async_wait_div();
     __syncthreads();
-    issue(i + DR - 1);  // into the slot read at iteration i - 1
-    const float* s = sm + (i % DR) * 6 * SPL + wbase;
-    auto w = [&](int comp, int r, int c) { return f2(s[comp * SPL + r * SW + c], s[(3 + comp) * SPL + r * SW + c]); };
-    float2 X[4][2], Y[4][3], Z[4][3];
+    issue(i + DRD - 1);  // into the slot read at iteration i - 1
+    const float* s = sm + (i % DRD) * 6 * SPLD + wbase;
+    auto w = [&](int comp, int r, int c) { return f2(s[comp * SPLD + r * SW + c], s[(3 + comp) * SPLD + r * SW + c]); };
+    // per row of the window: the x-part delta_x v_x, and s_x of v_y and of v_z
+    float2 xd[USD + 2], ys[USD + 2], zs[USD + 2];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      X[r][0] = w(0, r, 0);
-      X[r][1] = w(0, r, 2);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        Y[r][c] = w(1, r, c);
-        Z[r][c] = w(2, r, c);
-      }
+    for (int r = 0; r < USD + 2; ++r) {
+      xd[r] = vsub(w(0, r, 2), w(0, r, 0));
+      ys[r] = vfma(four, w(1, r, 1), vadd(w(1, r, 0), w(1, r, 2)));
+      zs[r] = vfma(four, w(2, r, 1), vadd(w(2, r, 0), w(2, r, 2)));
     }
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      const float2 xr = vsub(vfma(four, X[k + 1][1], vadd(X[k][1], X[k + 2][1])),
-                             vfma(four, X[k + 1][0], vadd(X[k][0], X[k + 2][0])));
-      const float2 yr = vfma(four, vsub(Y[k + 2][1], Y[k][1]), vadd(vsub(Y[k + 2][0], Y[k][0]), vsub(Y[k + 2][2], Y[k][2])));
-      const float2 t0 = vfma(four, Z[k + 1][0], vadd(Z[k][0], Z[k + 2][0]));
-      const float2 t1 = vfma(four, Z[k + 1][1], vadd(Z[k][1], Z[k + 2][1]));
-      const float2 t2 = vfma(four, Z[k + 1][2], vadd(Z[k][2], Z[k + 2][2]));
-      const float2 zr = vfma(four, t1, vadd(t0, t2));
+    for (int k = 0; k < USD; ++k) {
+      const float2 xr = vfma(four, xd[k + 1], vadd(xd[k], xd[k + 2]));  // delta_x s_y v_x
+      const float2 yr = vsub(ys[k + 2], ys[k]);                          // s_x delta_y v_y
+      const float2 zr = vfma(four, zs[k + 1], vadd(zs[k], zs[k + 2]));   // s_x s_y v_z
       const float2 Q = vadd(xr, yr);
       const float2 dv = vadd(vadd(rD1[k], Q), zr);
       rD1[k] = vfma(four, Q, rD2[k]);
@@ -745,7 +746,7 @@ dim3 grid_for(const Group<float>& g, int zc, int& nchunk) {
 
 }  // namespace
 
-bool fused_supported(int N) { return N >= 32 && N % TX == 0 && N % TY == 0; }
+bool fused_supported(int N) { return N >= 32 && N % TX == 0 && N % TY == 0 && N % TYD == 0; }
 
 void fused_prepare() {
   check(cudaFuncSetAttribute(k_fused_rhs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RHS_SMEM),
@@ -766,6 +767,7 @@ void launch_fused_rhs(const Group<float>& g, int par, cudaStream_t st) {
 void launch_fused_div(const Group<float>& g, int par, cudaStream_t st) {
   int nchunk;
   dim3 grid = grid_for(g, g.zc[1], nchunk);
+  grid.y = g.N / TYD;
   k_fused_div<<<grid, NTV, DIV_SMEM, st>>>(g.d_inst, par, nchunk, g.zc[1]);
   check(cudaGetLastError(), "fused_div launch");
 }
