@@ -710,33 +710,38 @@ void append_cache(const char* path, const std::string& key, const ttsh_tuning& t
 
 }  // namespace
 
-// Host (FP64) <-> device (T) copies of one N^3 field.
+// Host (FP64) <-> device (T) copies of one N^3 field, asynchronous on `st` (the caller
+// synchronises). For FP32 fields the FP64 data crosses the bus as it is and is converted on the
+// device through `scratch`: n doubles of device memory that no step reads (the other half of the
+// u* ping-pong pair, which the next step overwrites before reading). Successive calls reuse it
+// in stream order.
 template <class T>
-static void h2d(T* dst, const double* src, size_t n, cudaStream_t st) {
-  if (sizeof(T) == sizeof(double)) {
+static void h2d(T* dst, const double* src, size_t n, cudaStream_t st, double* scratch) {
+  if constexpr (sizeof(T) == sizeof(double)) {
     CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, st));
-    CK(cudaStreamSynchronize(st));
   } else {
-    std::vector<T> tmp(n);
-    for (size_t i = 0; i < n; ++i) tmp[i] = (T)src[i];
-    CK(cudaMemcpyAsync(dst, tmp.data(), n * sizeof(T), cudaMemcpyHostToDevice, st));
-    CK(cudaStreamSynchronize(st));
+    CK(cudaMemcpyAsync(scratch, src, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    launch_to_f32(scratch, dst, n, st);
   }
 }
 template <class T>
-static void d2h(double* dst, const T* src, size_t n, cudaStream_t st, size_t stride = 1) {
-  if (sizeof(T) == sizeof(double) && stride == 1) {
-    CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
+static void d2h(double* dst, const T* src, size_t n, cudaStream_t st, double* scratch, size_t stride = 1) {
+  if constexpr (sizeof(T) == sizeof(double)) {
+    if (stride == 1) CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    else CK(cudaMemcpy2DAsync(dst, sizeof(double), src, stride * sizeof(double), sizeof(double), n,
+                              cudaMemcpyDeviceToHost, st));
   } else {
-    // the span from the first to the last strided element only: the odd component of an
-    // interleaved array ends one element before the array does
-    const size_t span = n == 0 ? 0 : (n - 1) * stride + 1;
-    std::vector<T> tmp(span);
-    if (span) CK(cudaMemcpyAsync(tmp.data(), src, span * sizeof(T), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    for (size_t i = 0; i < n; ++i) dst[i] = (double)tmp[i * stride];
+    launch_to_f64(src, stride, scratch, n, st);
+    CK(cudaMemcpyAsync(dst, scratch, n * sizeof(double), cudaMemcpyDeviceToHost, st));
   }
+}
+// The conversion scratch of an instance: its u* buffer of the parity not in use (three
+// consecutive arena slots, >= 12 N^3 bytes), or nullptr for FP64 fields.
+template <class I_>
+static double* conv_scratch(const ttsh_sim* s, const I_& I) {
+  typedef typename std::decay<decltype(*I.phi[0])>::type TT;
+  if constexpr (std::is_same<TT, float>::value) return reinterpret_cast<double*>(I.Us[s->par ^ 1][0]);
+  else return nullptr;
 }
 
 // The 13 state arrays of a checkpoint, in file order, as device pointers of the current parity.
@@ -862,14 +867,15 @@ int ttsh_set_state(ttsh_sim* s, int inst, const double* phi, const double* P, co
     s->with_engine([&](auto& E) {
       auto& I = E.h[inst];
       typedef typename std::decay<decltype(*I.phi[0])>::type TT;
-      h2d<TT>(I.phi[s->par], phi, n, s->stream);
+      double* scr = conv_scratch(s, I);
+      h2d<TT>(I.phi[s->par], phi, n, s->stream, scr);
       if (I.phic) CK(cudaMemsetAsync(I.phic, 0, n * sizeof(TT), s->stream));
       for (int b = 0; b < 3; ++b) {
-        h2d<TT>(I.P[b], P + b * n, n, s->stream);
-        h2d<TT>(I.U[b], u + b * n, n, s->stream);
-        if (ustar) h2d<TT>(I.Us[s->par][b], ustar + b * n, n, s->stream);
+        h2d<TT>(I.P[b], P + b * n, n, s->stream, scr);
+        h2d<TT>(I.U[b], u + b * n, n, s->stream, scr);
+        if (ustar) h2d<TT>(I.Us[s->par][b], ustar + b * n, n, s->stream, scr);
         else CK(cudaMemsetAsync(I.Us[s->par][b], 0, n * sizeof(TT), s->stream));
-        if (Pstar) h2d<TT>(I.Ps[s->par][b], Pstar + b * n, n, s->stream);
+        if (Pstar) h2d<TT>(I.Ps[s->par][b], Pstar + b * n, n, s->stream, scr);
         else CK(cudaMemsetAsync(I.Ps[s->par][b], 0, n * sizeof(TT), s->stream));
       }
       CK(cudaStreamSynchronize(s->stream));
@@ -912,14 +918,16 @@ int ttsh_get_state(ttsh_sim* s, int inst, double* phi, double* P, double* u, dou
     s->with_engine([&](auto& E) {
       auto& I = E.h[inst];
       typedef typename std::decay<decltype(*I.phi[0])>::type TT;
-      if (phi) d2h<TT>(phi, I.phi[s->par], n, s->stream);
+      double* scr = conv_scratch(s, I);
+      if (phi) d2h<TT>(phi, I.phi[s->par], n, s->stream, scr);
       for (int b = 0; b < 3; ++b) {
-        if (P) d2h<TT>(P + b * n, I.P[b], n, s->stream);
-        if (u) d2h<TT>(u + b * n, I.U[b], n, s->stream);
+        if (P) d2h<TT>(P + b * n, I.P[b], n, s->stream, scr);
+        if (u) d2h<TT>(u + b * n, I.U[b], n, s->stream, scr);
       }
       const TT* w = reinterpret_cast<const TT*>(I.W);
-      if (p_v) d2h<TT>(p_v, w, n, s->stream, 2);
-      if (p_p) d2h<TT>(p_p, w + 1, n, s->stream, 2);
+      if (p_v) d2h<TT>(p_v, w, n, s->stream, scr, 2);
+      if (p_p) d2h<TT>(p_p, w + 1, n, s->stream, scr, 2);
+      CK(cudaStreamSynchronize(s->stream));
     });
     return TTSH_OK;
   });
@@ -937,9 +945,10 @@ int ttsh_get_provisional(ttsh_sim* s, int inst, double* ustar, double* Pstar) {
       auto& I = E.h[inst];
       typedef typename std::decay<decltype(*I.phi[0])>::type TT;
       for (int b = 0; b < 3; ++b) {
-        if (ustar) d2h<TT>(ustar + b * n, I.Us[s->par][b], n, s->stream);
-        if (Pstar) d2h<TT>(Pstar + b * n, I.Ps[s->par][b], n, s->stream);
+        if (ustar) d2h<TT>(ustar + b * n, I.Us[s->par][b], n, s->stream, conv_scratch(s, I));
+        if (Pstar) d2h<TT>(Pstar + b * n, I.Ps[s->par][b], n, s->stream, conv_scratch(s, I));
       }
+      CK(cudaStreamSynchronize(s->stream));
     });
     return TTSH_OK;
   });

@@ -181,8 +181,33 @@ __global__ void __launch_bounds__(BX* BY) k_correct(const InstDev<T>* __restrict
 
 constexpr int STATS_BLOCKS = 256, STATS_THREADS = 256;
 
-// FP64 diagnostics of the current state (phi[par], u, P): per block, sum(phi),
-// max |D.u|, max |u|, and a non-finite count. Fixed reduction order.
+// Diagnostics of the current state (phi[par], u, P): per block, sum(phi), max |D.u|, max |u|, and
+// a non-finite count, combined across threads and blocks in FP64 in a fixed order. FP64 fields
+// are summed in FP64. FP32 fields are summed by each thread in FP32 with Kahan's compensated
+// summation (error of order one rounding of the thread's partial, instead of one per term) and
+// only the per-thread partials are combined in FP64: the GPU's FP64 rate is a small fraction of
+// its FP32 rate, and an FP64 add per site would cost more than the step's stencils for a mass
+// read-back after every step. The maxima are exact in either precision.
+template <class T>
+struct MassAcc;
+template <>
+struct MassAcc<double> {
+  double s = 0;
+  __device__ __forceinline__ void add(double v) { s += v; }
+  __device__ __forceinline__ double total() const { return s; }
+};
+template <>
+struct MassAcc<float> {
+  float s = 0.f, c = 0.f;  // Kahan: c carries the low part lost by the last addition
+  __device__ __forceinline__ void add(float v) {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double total() const { return (double)s - (double)c; }
+};
+
 template <class T, bool FULL>
 __global__ void __launch_bounds__(STATS_THREADS) k_stats(const InstDev<T>* __restrict__ insts, int par) {
   const InstDev<T>& I = insts[blockIdx.y];
@@ -190,24 +215,26 @@ __global__ void __launch_bounds__(STATS_THREADS) k_stats(const InstDev<T>* __res
   const long n = (long)N * N * N;
   const Phys<T>& p = I.ph;
   const T* phi = I.phi[par];
-  double sum = 0, mdiv = 0, mu = 0, bad = 0;
+  MassAcc<T> acc;
+  T mdivT = 0, muT = 0;
+  int badn = 0;
   for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const T ph = phi[i];
+    acc.add(ph);
+    if (!isfinite(ph)) badn += 1;
+    if (!FULL) continue;
     const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / ((long)N * N));
     Site s;
-    if (FULL) s.init(x, y, z, N);
-    const double ph = (double)phi[i];
-    sum += ph;
-    if (!isfinite(ph)) bad += 1;
-    if (!FULL) continue;
-    const double d = (double)st_dx<T>(s.acc<T>(I.U[0]), p.c2h) + (double)st_dy<T>(s.acc<T>(I.U[1]), p.c2h) +
-                     (double)st_dz<T>(s.acc<T>(I.U[2]), p.c2h);
-    mdiv = fmax(mdiv, fabs(d));
+    s.init(x, y, z, N);
+    const T d = st_dx<T>(s.acc<T>(I.U[0]), p.c2h) + st_dy<T>(s.acc<T>(I.U[1]), p.c2h) + st_dz<T>(s.acc<T>(I.U[2]), p.c2h);
+    mdivT = fmax(mdivT, fabs(d));
     for (int b = 0; b < 3; ++b) {
-      const double u = (double)I.U[b][i], q = (double)I.P[b][i];
-      mu = fmax(mu, fabs(u));
-      if (!isfinite(u) || !isfinite(q)) bad += 1;
+      const T u = I.U[b][i], q = I.P[b][i];
+      muT = fmax(muT, fabs(u));
+      if (!isfinite(u) || !isfinite(q)) badn += 1;
     }
   }
+  double sum = acc.total(), mdiv = (double)mdivT, mu = (double)muT, bad = (double)badn;
   __shared__ double sh[4][STATS_THREADS / 32];
   for (int o = 16; o > 0; o >>= 1) {
     sum += __shfl_down_sync(0xffffffffu, sum, o);

@@ -78,7 +78,30 @@ __global__ void k_slice(const InstDev<T>* __restrict__ insts, int inst, int par,
   out[8 * NN + o] = dx(I.P[1]) - dy(I.P[0]);  // Pvortex = d1xO4(py) - d1yO4(px) (readDraw.py:237)
 }
 
+// FP64 <-> FP32 conversion of one field on the device, for the host interface of the FP32 forms:
+// the caller's FP64 arrays are copied as they are and converted here (round to nearest), instead
+// of being converted element by element on the host.
+__global__ void k_to_f32(const double* __restrict__ src, float* __restrict__ dst, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = __double2float_rn(src[i]);
+}
+__global__ void k_to_f64(const float* __restrict__ src, size_t stride, double* __restrict__ dst, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = (double)src[i * stride];
+}
+
 }  // namespace
+
+void launch_to_f32(const double* src, float* dst, size_t n, cudaStream_t st) {
+  k_to_f32<<<1216, 256, 0, st>>>(src, dst, n);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) throw std::runtime_error(std::string("conversion launch: ") + cudaGetErrorString(e));
+}
+void launch_to_f64(const float* src, size_t stride, double* dst, size_t n, cudaStream_t st) {
+  k_to_f64<<<1216, 256, 0, st>>>(src, stride, dst, n);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) throw std::runtime_error(std::string("conversion launch: ") + cudaGetErrorString(e));
+}
 
 int centroid_blocks() { return CB; }
 
