@@ -1122,6 +1122,16 @@ int ttsh_run_dirs(const char* const* dirs, int n, const ttsh_ext* ext, uint64_t 
     }
     run[i] = {p.T0, p.dt0, p.dte, p.Ts, true};
   }
+  // opt-in autotuning (TTSH_TUNE=1; TTSH_TUNE_CACHE names a cache file), on the initial fields
+  if (const char* tv = std::getenv("TTSH_TUNE")) {
+    if (std::atoi(tv) != 0) {
+      int rt = ttsh_autotune(s, std::getenv("TTSH_TUNE_CACHE"));
+      if (rt) {
+        ttsh_destroy(s);
+        return rt;
+      }
+    }
+  }
   // evolve() of every droplet in lockstep (TTSH3D.cu:311-331): advance to the nearest event
   for (;;) {
     int nact = 0;

@@ -65,6 +65,7 @@ struct Api {
   const char* (*last_error)(void);
   int (*struct_size)(int);
   int (*init_reference)(const ttsh_input*, unsigned, const char*, double*, double*, double*, double*, double*);
+  int (*autotune)(ttsh_sim*, const char*);
 };
 
 static void* load_lib() {
@@ -165,6 +166,14 @@ int main() {
   if (rc != 0) {
     cout << "TTSH3D: " << a.last_error() << endl;
     return 2;
+  }
+  // opt-in kernel autotuning on the initial fields (TTSH_TUNE=1; TTSH_TUNE_CACHE: cache file)
+  if (env_i("TTSH_TUNE", 0) != 0) {
+    if (!sym(h, "ttsh_autotune", a.autotune)) return 1;
+    if ((rc = a.autotune(sim, getenv("TTSH_TUNE_CACHE"))) != 0) {
+      cout << "TTSH3D: " << a.last_error() << endl;
+      return 2;
+    }
   }
   // evolve (TTSH3D.cu:290-332); steps between snapshots are issued as one call.
   double T = P.T0, Dt = P.dt0;

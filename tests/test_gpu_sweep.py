@@ -44,3 +44,33 @@ def test_init_reference_is_deterministic():
     assert all(np.array_equal(a[k], b[k]) for k in a)
     assert not np.array_equal(a["u"], c["u"])
     assert np.abs(a["u"]).max() <= 0.5e-4 + 1e-18
+
+
+def test_run_dirs_with_autotuning(tmp_path, monkeypatch):
+    """TTSH_TUNE=1 makes the sweep driver tune the batch on its initial fields and record the
+    choices in TTSH_TUNE_CACHE; the snapshots agree with untuned runs (the FFT choice changes
+    FP64 rounding only)."""
+    import numpy as np
+    import ttsh
+    specs = [dict(Nx=16, Ny=16, Nz=16, Ts=0.009, dte=0.004), dict(Nx=24, Ny=24, Nz=24, Ts=0.007, dte=0.004)]
+    tuned = [str(tmp_path / ("t%d" % i)) for i in range(len(specs))]
+    plain = [str(tmp_path / ("p%d" % i)) for i in range(len(specs))]
+    for i, sp in enumerate(specs):
+        _make(tuned[i], **sp)
+        _make(plain[i], **sp)
+    cache = str(tmp_path / "tune.txt")
+    monkeypatch.setenv("TTSH_TUNE", "1")
+    monkeypatch.setenv("TTSH_TUNE_CACHE", cache)
+    ttsh.run_dirs(tuned, seed=7)
+    monkeypatch.delenv("TTSH_TUNE")
+    monkeypatch.delenv("TTSH_TUNE_CACHE")
+    ttsh.run_dirs(plain, seed=7)
+    lines = open(cache).read().splitlines()
+    assert len(lines) == 2 and all(" N16 " in l or " N24 " in l for l in lines), lines
+    for i in range(len(specs)):
+        files = sorted(f for f in os.listdir(plain[i]) if f.startswith("conf_"))
+        assert files == sorted(f for f in os.listdir(tuned[i]) if f.startswith("conf_")) and len(files) >= 2
+        for f in files:
+            a = np.loadtxt(os.path.join(tuned[i], f))
+            b = np.loadtxt(os.path.join(plain[i], f))
+            np.testing.assert_allclose(a, b, rtol=0, atol=1e-12)
