@@ -92,3 +92,41 @@ def test_fused_discrete_k2_divergence_small():
     f = run(st, 50, ttsh.FORM_FUSED, k2_mode=1, quirks=0, zeta=0.02)
     umax = np.abs(f["u"]).max()
     assert f["stats"]["max_div_u"] <= 1e-5 * max(umax, 1e-3), (f["stats"], umax)
+
+
+def test_fused_fp32_vs_fp64_at_256():
+    """The headline size: one 256^3 droplet (R = 64, xi = 2, seed 1, zeta = 0.02), 200 steps, FP32
+    fused form against the FP64 form. phi, P, u within the 1e-5 relative L2 target (measured after
+    1000 steps: 2e-8, 4e-7, 5e-7); the FP32 mass drift within 2x of the FP64 form's (the phi
+    update is compensated)."""
+    import ttsh
+    st = droplet_state(256, seed=1)
+    outs = {}
+    for prec, form in ((64, ttsh.FORM_PLAIN), (32, ttsh.FORM_FUSED)):
+        outs[prec] = run(st, 200, form, precision=prec, zeta=0.02)
+    errs = field_errors(outs[32], outs[64])
+    for k in ("phi", "P", "u"):
+        assert errs[k] <= 1e-5, errs
+    m0 = st["phi"].sum()
+    d32 = (outs[32]["stats"]["mass"] - m0) / m0
+    d64 = (outs[64]["stats"]["mass"] - m0) / m0
+    assert abs(d32 - d64) <= max(abs(d64), 1e-9), (d32, d64)
+
+
+def test_fused_fp32_at_512():
+    """The largest configuration (512^3, R = 160, xi = 3, seed 7, zeta = 0.02, discrete k^2):
+    20 steps stay finite, the mass changes by the scheme's drift only, and the projected velocity
+    is solenoidal to FP32 round-off."""
+    import ttsh
+    N = 512
+    phi, P = ttsh.init_droplet(N, 160.0, 3.0, 7, angular_noise=0.01)
+    inp = ttsh.default_input(Nx=N, Ny=N, Nz=N)
+    ext = ttsh.default_ext(precision=32, zeta=0.02, k2_mode=1, quirks=0, form=ttsh.FORM_FUSED)
+    with ttsh.Sim(inp, ext) as s:
+        s.set_state(0, phi, P, np.zeros_like(P))
+        m0 = s.reduce(0)["mass"]
+        s.step(20)
+        st = s.reduce(0)
+    assert st["nonfinite"] == 0
+    assert abs(st["mass"] - m0) <= 1e-6 * m0, (st["mass"], m0)
+    assert st["max_div_u"] <= 1e-5 * max(st["max_abs_u"], 1e-3), st
