@@ -39,7 +39,7 @@ namespace ttsh {
 namespace {
 
 constexpr int TX = 32, TY = 16;   // output tile (columns)
-constexpr int RB = 2;             // strip length (sites per thread) of fused_rhs stage 1
+constexpr int RB = 3;             // strip length (sites per thread) of fused_rhs stage 1 (a 5-row window)
 constexpr int NT = 512;           // threads of fused_rhs: one tile column each in phase 2
 constexpr int US = 4;             // strip length of the velocity terms (phase 1)
 
@@ -74,7 +74,7 @@ constexpr size_t RHS_SMEM = OFF_PQ + (size_t)2 * NPQ * CNP * sizeof(float2);
 static_assert(OFF_U01 % 16 == 0 && OFF_U2 % 16 == 0 && OFF_PR % 16 == 0 && OFF_SZX % 16 == 0 && OFF_PQ % 16 == 0,
               "16-byte aligned regions");
 // phase-1 thread roles of fused_rhs: stage-1 strips of the B region, then the velocity strips
-constexpr int NS1 = (BW * BH) / RB;                   // 306 stage-1 strips
+constexpr int NS1 = (BW * BH) / RB;                   // 204 stage-1 strips
 constexpr int NU0 = ((NS1 + 31) / 32) * 32;           // first velocity thread (warp aligned)
 constexpr int NUS = TX * (TY / US);                   // 128 velocity strips
 static_assert((BH % RB) == 0 && (TY % US) == 0, "strip lengths divide the regions");
