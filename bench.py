@@ -63,7 +63,7 @@ KERNEL_WORDS = {
 # of one ncu capture on a 256^3 droplet (--set full, --clock-control none); a launch over more
 # sites scales with the sites (every kernel streams its planes once).
 TRAFFIC_BYTES_PER_SITE_F32 = {
-    "fused_rhs": (557.171968e6 + 497.317888e6) / 256 ** 3,
+    "fused_rhs": (557.067264e6 + 493.400832e6) / 256 ** 3,
 }
 
 
