@@ -757,6 +757,37 @@ static std::vector<void*> state_arrays(ttsh_sim* s, E& eng, int inst) {
   return a;
 }
 
+// Host-side reduction of one group's diagnostics partials (per droplet: blocks x {sum, max|D.u|,
+// max|u|, non-finite count}, fixed order) into ttsh_stats; returns whether any value is non-finite.
+template <class E>
+static bool stats_of_group(const ttsh_sim* s, const E& eng, size_t g, int what, const double* part, int64_t steps,
+                           const double* T, ttsh_stats* out) {
+  const size_t per = 4 * (size_t)stats_partials_per_instance(0);
+  bool bad_any = false;
+  for (size_t k = 0; k < eng.members[g].size(); ++k) {
+    const int inst = eng.members[g][k];
+    double sum = 0, md = 0, mu = 0, bad = 0;
+    for (size_t b = 0; b < per / 4; ++b) {
+      const double* q = &part[k * per + 4 * b];
+      sum += q[0];
+      md = std::max(md, q[1]);
+      mu = std::max(mu, q[2]);
+      bad += q[3];
+    }
+    const double h = s->inst[inst].in.h;
+    ttsh_stats& o = out[inst];
+    o.mass = sum * h * h * h;
+    o.max_div_u = what == TTSH_STATS_ALL ? md : -1.0;
+    o.max_abs_u = what == TTSH_STATS_ALL ? mu : -1.0;
+    o.T = T[inst];
+    o.steps = steps;
+    o.nonfinite = bad > 0 ? 1 : 0;
+    o.reserved = 0;
+    if (bad > 0) bad_any = true;
+  }
+  return bad_any;
+}
+
 extern "C" {
 
 int ttsh_batch_create(const ttsh_input* in, const ttsh_ext* ext, int n, int device, ttsh_sim** out) {
@@ -994,7 +1025,9 @@ int ttsh_reduce_all(ttsh_sim* s, int what, ttsh_stats* out) {
   if (what != TTSH_STATS_ALL && what != TTSH_STATS_MASS) return set_error(TTSH_E_INVALID, "bad stats selector");
   return guarded([&]() -> int {
     CK(cudaSetDevice(s->device));
-    int bad_any = 0;
+    bool bad_any = false;
+    std::vector<double> T(s->inst.size());
+    for (size_t i = 0; i < T.size(); ++i) T[i] = s->inst[i].T;
     s->with_engine([&](auto& E) {
       const size_t per = 4 * (size_t)stats_partials_per_instance(0);
       for (size_t g = 0; g < E.groups.size(); ++g) {
@@ -1003,31 +1036,62 @@ int ttsh_reduce_all(ttsh_sim* s, int what, ttsh_stats* out) {
         std::vector<double> part(per * G.n);
         CK(cudaMemcpyAsync(part.data(), G.red, part.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
-        for (int k = 0; k < G.n; ++k) {
-          const int inst = E.members[g][k];
-          double sum = 0, md = 0, mu = 0, bad = 0;
-          for (size_t b = 0; b < per / 4; ++b) {
-            const double* q = &part[k * per + 4 * b];
-            sum += q[0];
-            md = std::max(md, q[1]);
-            mu = std::max(mu, q[2]);
-            bad += q[3];
-          }
-          const double h = s->inst[inst].in.h;
-          ttsh_stats& o = out[inst];
-          o.mass = sum * h * h * h;
-          o.max_div_u = what == TTSH_STATS_ALL ? md : -1.0;
-          o.max_abs_u = what == TTSH_STATS_ALL ? mu : -1.0;
-          o.T = s->inst[inst].T;
-          o.steps = s->steps;
-          o.nonfinite = bad > 0 ? 1 : 0;
-          o.reserved = 0;
-          if (bad > 0) bad_any = 1;
-        }
+        if (stats_of_group(s, E, g, what, part.data(), s->steps, T.data(), out)) bad_any = true;
       }
     });
     return bad_any ? set_error(TTSH_E_UNSTABLE, "non-finite values in the state") : TTSH_OK;
   });
+}
+
+// Layout of an asynchronous diagnostics buffer: [steps, what, T of each droplet, then the
+// partials of every group in group order].
+static size_t partials_doubles(const ttsh_sim* s) {
+  size_t n = 2 + s->inst.size();
+  const size_t per = 4 * (size_t)stats_partials_per_instance(0);
+  return n + per * s->inst.size();
+}
+
+size_t ttsh_partials_size(const ttsh_sim* s) { return s ? partials_doubles(s) : 0; }
+
+int ttsh_reduce_all_async(ttsh_sim* s, int what, double* partials) {
+  if (!s || !partials) return set_error(TTSH_E_INVALID, "null argument");
+  if (what != TTSH_STATS_ALL && what != TTSH_STATS_MASS) return set_error(TTSH_E_INVALID, "bad stats selector");
+  return guarded([&]() -> int {
+    CK(cudaSetDevice(s->device));
+    partials[0] = (double)s->steps;
+    partials[1] = (double)what;
+    for (size_t i = 0; i < s->inst.size(); ++i) partials[2 + i] = s->inst[i].T;
+    double* dst = partials + 2 + s->inst.size();
+    s->with_engine([&](auto& E) {
+      const size_t per = 4 * (size_t)stats_partials_per_instance(0);
+      for (size_t g = 0; g < E.groups.size(); ++g) {
+        const auto& G = E.groups[g];
+        launch_stats(G, s->par, s->stream, what == TTSH_STATS_ALL);
+        CK(cudaMemcpyAsync(dst, G.red, per * G.n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        dst += per * G.n;
+      }
+    });
+    return TTSH_OK;
+  });
+}
+
+int ttsh_stats_from_partials(const ttsh_sim* s, const double* partials, ttsh_stats* out) {
+  if (!s || !partials || !out) return set_error(TTSH_E_INVALID, "null argument");
+  const int what = (int)partials[1];
+  if (what != TTSH_STATS_ALL && what != TTSH_STATS_MASS) return set_error(TTSH_E_INVALID, "not a diagnostics buffer");
+  bool bad_any = false;
+  const double* T = partials + 2;
+  const double* part = partials + 2 + s->inst.size();
+  const size_t per = 4 * (size_t)stats_partials_per_instance(0);
+  auto run = [&](const auto& E) {
+    for (size_t g = 0; g < E.groups.size(); ++g) {
+      if (stats_of_group(s, E, g, what, part, (int64_t)partials[0], T, out)) bad_any = true;
+      part += per * E.groups[g].n;
+    }
+  };
+  if (s->precision == 32) run(s->ef);
+  else run(s->ed);
+  return bad_any ? set_error(TTSH_E_UNSTABLE, "non-finite values in the state") : TTSH_OK;
 }
 
 int ttsh_write_conf(ttsh_sim* s, int inst, const char* path) {

@@ -135,6 +135,9 @@ def lib():
                                ctypes.c_int], ctypes.c_int),
             "ttsh_snapshot_slice": ([_VP, ctypes.c_int, _D, ctypes.POINTER(ctypes.c_int), _D], ctypes.c_int),
             "ttsh_load_checkpoint": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),
+            "ttsh_partials_size": ([_VP], ctypes.c_size_t),
+            "ttsh_reduce_all_async": ([_VP, ctypes.c_int, _D], ctypes.c_int),
+            "ttsh_stats_from_partials": ([_VP, _D, ctypes.POINTER(Stats)], ctypes.c_int),
             "ttsh_num_groups": ([_VP], ctypes.c_int),
             "ttsh_get_tuning": ([_VP, ctypes.c_int, ctypes.POINTER(Tuning)], ctypes.c_int),
             "ttsh_set_tuning": ([_VP, ctypes.c_int, ctypes.POINTER(Tuning)], ctypes.c_int),
@@ -316,6 +319,23 @@ class Sim:
         if check or rc != E_UNSTABLE:
             _check(rc)
         return st.as_dict()
+
+    def partials_size(self) -> int:
+        return int(lib().ttsh_partials_size(self._h))
+
+    def reduce_all_async(self, buf, mass_only: bool = False):
+        """Enqueue the diagnostics of every droplet into `buf` (float64, contiguous, at least
+        partials_size() values; page-locked for an asynchronous copy) without waiting."""
+        assert buf.dtype == np.float64 and buf.flags.c_contiguous and buf.size >= self.partials_size()
+        _check(lib().ttsh_reduce_all_async(self._h, 1 if mass_only else 0, buf.ctypes.data_as(_D)))
+
+    def stats_from_partials(self, buf, check: bool = True):
+        """Per-droplet diagnostics of a buffer filled by reduce_all_async (after sync())."""
+        arr = (Stats * self.n)()
+        rc = lib().ttsh_stats_from_partials(self._h, buf.ctypes.data_as(_D), arr)
+        if check or rc != E_UNSTABLE:
+            _check(rc)
+        return [a.as_dict() for a in arr]
 
     def reduce_all(self, mass_only: bool = False, check: bool = True):
         """FP64 diagnostics of every droplet (one pass per size group, one copy back)."""

@@ -153,6 +153,18 @@ int ttsh_reduce(ttsh_sim* s, int inst, ttsh_stats* out);
 #define TTSH_STATS_MASS 1
 int ttsh_reduce_all(ttsh_sim* s, int what, ttsh_stats* out);
 
+/* Asynchronous form of ttsh_reduce_all for diagnostics recorded every step without stalling
+ * the GPU (the reference prints nothing per step; its ExpoConf, TTSH3D.cu:899-1014, is the only
+ * read-back): enqueues the diagnostics of every droplet on the handle's stream and their copy
+ * into `partials` (caller-owned host memory of ttsh_partials_size(s) doubles; page-locked memory
+ * makes the copy asynchronous), and returns without waiting. After ttsh_sync (or any call that
+ * waits for the stream), ttsh_stats_from_partials turns a filled buffer into per-droplet
+ * ttsh_stats, whose steps and T are the values at the call. A buffer must not be reused before its
+ * copy has completed. */
+size_t ttsh_partials_size(const ttsh_sim* s);
+int ttsh_reduce_all_async(ttsh_sim* s, int what, double* partials);
+int ttsh_stats_from_partials(const ttsh_sim* s, const double* partials, ttsh_stats* out);
+
 /* ExpoConf (TTSH3D.cu:899-1014): write the snapshot text file of instance `inst` at `path`:
  * one line per site, y outer, x, z inner; columns "vx vy vz px py pz phi" printed as
  * fixed with 15 decimals (ExpoData == 1) or "vx vy " (ExpoData == -1). */

@@ -200,3 +200,37 @@ def test_reduce_all_matches_single_reduce():
     for a, b, m in zip(one, allf, mass):
         assert a == b
         assert m["mass"] == a["mass"] and m["nonfinite"] == 0 and m["max_div_u"] == -1.0
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_reduce_all_async_matches_reduce_all(precision):
+    """ttsh_reduce_all_async + ttsh_stats_from_partials give ttsh_reduce_all's values, bit for
+    bit, for buffers filled at different steps and read only after one final sync."""
+    import torch
+    import ttsh
+    sizes = [32, 48, 32] if precision == 32 else [16, 24, 16]
+    states = [random_state(N, seed=70 + i) for i, N in enumerate(sizes)]
+    inps = [ttsh.default_input(Nx=N, Ny=N, Nz=N) for N in sizes]
+
+    def run(async_mode):
+        with ttsh.Sim(inps, [ttsh.default_ext(precision=precision) for _ in sizes]) as s:
+            for i, st in enumerate(states):
+                s.set_state(i, st["phi"], st["P"], st["u"])
+            if not async_mode:
+                out = []
+                for k in range(4):
+                    s.step(1)
+                    out.append(s.reduce_all(mass_only=(k % 2 == 1)))
+                return out
+            m = s.partials_size()
+            assert m > 2 + len(sizes)
+            bufs = torch.empty((4, m), dtype=torch.float64, pin_memory=True).numpy()
+            for k in range(4):
+                s.step(1)
+                s.reduce_all_async(bufs[k], mass_only=(k % 2 == 1))
+            s.sync()
+            return [s.stats_from_partials(bufs[k]) for k in range(4)]
+
+    got, want = run(True), run(False)
+    assert got == want
+    assert [g[0]["steps"] for g in got] == [1, 2, 3, 4]
