@@ -186,6 +186,7 @@ struct ttsh_sim {
   std::vector<void*> tables;  // shared per-N tables
   double* post = nullptr;     // snapshot-reduction scratch (allocated on first use)
   size_t post_bytes = 0;
+  int* d_err = nullptr;       // device word set by a kernel whose bounded wait ran out
 
   template <class F>
   void with_engine(F&& f) {
@@ -331,6 +332,11 @@ void build_engine(ttsh_sim* s, Engine<T>& E) {
     }
     I.W = reinterpret_cast<C*>(d + off);
   }
+  if (!s->d_err) {
+    CK(cudaMalloc(&s->d_err, sizeof(int)));
+    CK(cudaMemset(s->d_err, 0, sizeof(int)));
+    s->tables.push_back(s->d_err);
+  }
   for (size_t g = 0; g < E.members.size(); ++g) {
     // FP64 diagnostics partials of all droplets of the group, contiguous (one copy back)
     const size_t per = 4 * (size_t)stats_partials_per_instance(0);
@@ -346,6 +352,18 @@ void build_engine(ttsh_sim* s, Engine<T>& E) {
     G.fft_kind = (fk && std::string(fk) == "stockham") ? 1 : ((fk && std::string(fk) == "separate") ? 0 : 2);
     G.n = (int)E.members[g].size();
     G.N = s->inst[E.members[g][0]].N;
+    G.d_err = s->d_err;
+    // FP32: the z pass with its input staged by the tensor memory accelerator where the size has
+    // it (TTSH_ZTMA=0: the z pass that loads its input directly)
+    const char* zt = std::getenv("TTSH_ZTMA");
+    if (std::is_same<T, float>::value && !(zt && std::string(zt) == "0")) {
+      std::vector<const void*> W;
+      for (int i : E.members[g]) W.push_back(E.h[i].W);
+      void* maps = nullptr;
+      G.zt_grid = fftreg_zt_setup(G.N, W, &maps);
+      if (maps) s->tables.push_back(maps);
+      G.d_tmz = maps;
+    }
     std::vector<InstDev<T>> arr;
     for (int i : E.members[g]) arr.push_back(E.h[i]);
     CK(cudaMalloc(&G.d_inst, sizeof(InstDev<T>) * arr.size()));
@@ -388,6 +406,14 @@ void release(ttsh_sim* s) {
   if (s->post) cudaFree(s->post);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
   delete s;
+}
+
+// TTSH_E_CUDA when a kernel's bounded wait for its staged input ran out since the handle was
+// created (the state is then invalid); call after the stream has been synchronised.
+int kernel_error(ttsh_sim* s) {
+  int e = 0;
+  if (s->d_err) CK(cudaMemcpy(&e, s->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  return e ? set_error(TTSH_E_CUDA, "a kernel's wait for its staged input timed out; the state is invalid") : TTSH_OK;
 }
 
 template <class F>
@@ -934,7 +960,7 @@ int ttsh_sync(ttsh_sim* s) {
   return guarded([&]() -> int {
     CK(cudaSetDevice(s->device));
     CK(cudaStreamSynchronize(s->stream));
-    return TTSH_OK;
+    return kernel_error(s);
   });
 }
 
@@ -960,7 +986,7 @@ int ttsh_get_state(ttsh_sim* s, int inst, double* phi, double* P, double* u, dou
       if (p_p) d2h<TT>(p_p, w + 1, n, s->stream, scr, 2);
       CK(cudaStreamSynchronize(s->stream));
     });
-    return TTSH_OK;
+    return kernel_error(s);
   });
 }
 

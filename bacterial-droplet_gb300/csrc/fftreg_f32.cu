@@ -20,4 +20,21 @@ void fftreg_prepare<float>(int N) {
   fftreg::reg_prepare<float>(N);
 }
 
+int fftreg_zt_setup(int N, const std::vector<const void*>& W, void** d_maps) {
+  *d_maps = nullptr;
+  const int grid = fftreg::reg_zt_prepare(N);
+  if (grid <= 0 || W.empty()) return 0;
+  std::vector<CUtensorMap> maps(W.size());
+  for (size_t i = 0; i < W.size(); ++i) fftreg::reg_zt_encode(N, W[i], &maps[i]);
+  void* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, maps.size() * sizeof(CUtensorMap));
+  if (e == cudaSuccess) e = cudaMemcpy(d, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    if (d) cudaFree(d);
+    throw std::runtime_error(std::string("fft (staged z) descriptors: ") + cudaGetErrorString(e));
+  }
+  *d_maps = d;
+  return grid;
+}
+
 }  // namespace ttsh

@@ -1,6 +1,9 @@
 // fftreg_impl.cuh — the register-resident FFT pass kernel and its size table, instantiated for
 // one arithmetic type by fftreg_f32.cu / fftreg_f64.cu (two translation units build in parallel).
 #pragma once
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <stdexcept>
 #include <string>
 
@@ -23,16 +26,24 @@ constexpr size_t smem_bytes(int axis) {
   return axis == 0 ? (size_t)LB * N1 * (N2 + 1) * sizeof(C) : (size_t)N1 * N2 * LB * sizeof(C);
 }
 
+struct NoOp {
+  __device__ __forceinline__ void operator()() const {}
+};
+
 // PASS: 0 forward x, 1 forward y, 2 forward z + Poisson multiplier + inverse z, 3 inverse y,
 // 4 inverse x scaled by 1/N^3. One call transforms line group g of the pass (LB lines) with the
-// CTA's threads; S is the CTA's shared memory.
-template <class T, int N1, int N2, int PASS>
-__device__ __forceinline__ void fft_lines(const InstDev<T>& I, int g, typename CxT<T>::type* S) {
+// CTA's threads; S is the CTA's shared memory. SIN (z pass only): the group's input is already in
+// shared memory, In[z * LB + line]; `after` runs once every thread has read it (In may then be
+// refilled).
+template <class T, int N1, int N2, int PASS, bool SIN = false, class F = NoOp>
+__device__ __forceinline__ void fft_lines(const InstDev<T>& I, int g, typename CxT<T>::type* S,
+                                          const typename CxT<T>::type* In = nullptr, F after = F()) {
   typedef typename CxT<T>::type C;
   constexpr int N = N1 * N2;
   constexpr int LB = lines_per_cta<N>();
   constexpr int OW = N1 / N2;  // k1 rows owned by each thread in the second step
   constexpr int axis = (PASS == 0 || PASS == 4) ? 0 : ((PASS == 1 || PASS == 3) ? 1 : 2);
+  static_assert(!SIN || axis == 2, "shared-memory input: z pass only");
   C* __restrict__ W = I.W;
   const C* tab = I.tw;
   const size_t NN = (size_t)N * N;
@@ -60,12 +71,18 @@ __device__ __forceinline__ void fft_lines(const InstDev<T>& I, int g, typename C
   if constexpr (FWD_FIRST) {
     // first step: thread n2 = j transforms x[N2*n1 + j], n1 < N1
     C v[N1];
+    if constexpr (SIN) {
 #pragma unroll
-    for (int n1 = 0; n1 < N1; ++n1) v[n1] = W[base + (size_t)(N2 * n1 + j) * stride];
+      for (int n1 = 0; n1 < N1; ++n1) v[n1] = In[(N2 * n1 + j) * LB + l];
+    } else {
+#pragma unroll
+      for (int n1 = 0; n1 < N1; ++n1) v[n1] = W[base + (size_t)(N2 * n1 + j) * stride];
+    }
     Dft<C, N1, false>::run(v, tab, N2);
 #pragma unroll
     for (int k1 = 0; k1 < N1; ++k1) S[sidx(k1, j)] = (k1 > 0 && j > 0) ? cmul(v[k1], tw<C, false>(tab, j * k1)) : v[k1];
     __syncthreads();
+    after();
 #pragma unroll
     for (int o = 0; o < OW; ++o) {
       const int k1 = j + N2 * o;
@@ -193,6 +210,144 @@ __global__ void __cluster_dims__(plane_parts<N1 * N2>(), 1, 1) __launch_bounds__
 template <class T, int N1, int N2>
 constexpr bool plane_hinted() { return sizeof(T) == 4 && N1 * N2 == 256; }
 
+// ---- the z pass with its input staged by the tensor memory accelerator (FP32) ----
+// Persistent CTAs: CTA b takes the z-line groups b, b + grid, ... of every droplet of the size
+// group. A group's input, the LB x 1 x N box (x, y, z) of the droplet's complex field, is copied
+// into one of ZST shared-memory stages by cp.async.bulk.tensor (one instruction per 256 z-planes),
+// ZST groups ahead of the one being transformed; an mbarrier per stage counts the bytes in.
+// Arithmetic and output are those of k_fftr<float, N1, N2, 2>.
+constexpr int ZST = 2;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Waits for phase `parity` of the barrier for at most 2^31 SM clocks (about a second); false when
+// that limit ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* b, unsigned parity) {
+  if (mbar_try_wait(b, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(b, parity))
+    if (clock64() - t0 > (1ll << 31)) return false;
+  return true;
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(
+          smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+template <int N>
+constexpr size_t zt_smem() {
+  return (size_t)(ZST + 1) * N * lines_per_cta<N>() * sizeof(float2) + ZST * sizeof(uint64_t);
+}
+template <int N>
+constexpr int zt_min_blocks() { return 2 * zt_smem<N>() <= 227 * 1024 ? 2 : 1; }
+// The sizes with the staged z pass: a CTA of at least 128 threads, one or two boxes per line.
+template <int N1, int N2>
+constexpr bool zt_has() {
+  return lines_per_cta<N1 * N2>() == 16 && N2 >= 8 && (N1 * N2 <= 256 || N1 * N2 == 512) && zt_smem<N1 * N2>() <= 227 * 1024;
+}
+
+template <int N1, int N2>
+__global__ void __launch_bounds__(lines_per_cta<N1 * N2>() * N2, zt_min_blocks<N1 * N2>())
+    k_fftz_tma(const InstDev<float>* __restrict__ insts, const CUtensorMap* __restrict__ maps, int ninst,
+               int* __restrict__ err) {
+  typedef float2 C;
+  constexpr int N = N1 * N2, LB = lines_per_cta<N>(), NGX = N / LB, NG = N * NGX;
+  constexpr int NBOX = (N + 255) / 256, BZ = N / NBOX;
+  static_assert(NBOX * BZ == N, "the boxes tile a line");
+  constexpr unsigned STAGE = (unsigned)(N * LB * sizeof(C));
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  C* In = reinterpret_cast<C*>(smem_raw);                   // [ZST][N][LB]: the box layout
+  C* S = In + (size_t)ZST * N * LB;                          // the transposes, N * LB
+  uint64_t* bar = reinterpret_cast<uint64_t*>(S + (size_t)N * LB);  // [ZST]
+  const int total = ninst * NG, tid = threadIdx.x;
+  auto issue = [&](int g, int s) {
+    const int inst = g / NG, gl = g - inst * NG;
+    const int y = gl / NGX, x = (gl - y * NGX) * LB;
+    mbar_expect_tx(&bar[s], STAGE);
+#pragma unroll
+    for (int b = 0; b < NBOX; ++b)
+      tma_load_3d(In + ((size_t)s * N + (size_t)b * BZ) * LB, maps + inst, 2 * x, y, b * BZ, &bar[s]);
+  };
+  if (tid == 0) {
+    for (int s = 0; s < ZST; ++s) mbar_init(&bar[s], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (tid == 0)
+    for (int s = 0; s < ZST; ++s)
+      if (blockIdx.x + s * gridDim.x < total) issue(blockIdx.x + s * gridDim.x, s);
+  int k = 0;
+  bool ok = true;
+  for (int g = blockIdx.x; g < total; g += gridDim.x, ++k) {
+    const int s = k % ZST;
+    // every thread observes the copy complete (acquire); the CTA goes on only if all did
+    ok = __syncthreads_and(mbar_wait_bounded(&bar[s], (unsigned)(k / ZST) & 1u)) != 0;
+    if (!ok) break;
+    const int inst = g / NG, gn = g + ZST * gridDim.x;
+    fft_lines<float, N1, N2, 2, true>(insts[inst], g - inst * NG, S, In + (size_t)s * N * LB, [&] {
+      if (tid == 0 && gn < total) issue(gn, s);
+    });
+  }
+  if (!ok) {
+    // a copy did not complete in time: report it and wait (bounded) for this CTA's copies still
+    // in flight, groups k .. k + ZST - 1, before the CTA's shared memory is released
+    if (tid == 0) {
+      atomicExch(err, 1);
+      for (int kk = k; kk < k + ZST; ++kk)
+        if (blockIdx.x + kk * gridDim.x < total) mbar_wait_bounded(&bar[kk % ZST], (unsigned)(kk / ZST) & 1u);
+    }
+    __syncthreads();
+  }
+}
+
+template <int N1, int N2>
+void launch_zt(const Group<float>& g, cudaStream_t st) {
+  constexpr int N = N1 * N2, LB = lines_per_cta<N>();
+  const int total = g.n * N * (N / LB);
+  const int grid = total < g.zt_grid ? total : g.zt_grid;
+  k_fftz_tma<N1, N2><<<grid, LB * N2, zt_smem<N>(), st>>>(g.d_inst, reinterpret_cast<const CUtensorMap*>(g.d_tmz),
+                                                          g.n, g.d_err);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) throw std::runtime_error(std::string("fft (staged z) launch: ") + cudaGetErrorString(e));
+}
+
+// CTAs of the staged z pass that fit on the device at once (0: the size has none).
+template <int N1, int N2>
+int zt_prepare() {
+  if constexpr (!zt_has<N1, N2>()) {
+    return 0;
+  } else {
+    constexpr int N = N1 * N2, LB = lines_per_cta<N>();
+    cudaError_t e = cudaFuncSetAttribute((const void*)k_fftz_tma<N1, N2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)zt_smem<N>());
+    if (e != cudaSuccess) throw std::runtime_error(std::string("fft (staged z) smem attribute: ") + cudaGetErrorString(e));
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_fftz_tma<N1, N2>, LB * N2, zt_smem<N>());
+    if (e != cudaSuccess) throw std::runtime_error(std::string("fft (staged z) occupancy: ") + cudaGetErrorString(e));
+    return sms * per;
+  }
+}
+
 template <class T, int N1, int N2, int PASS>
 void launch_pass(const Group<T>& g, cudaStream_t st) {
   constexpr int N = N1 * N2;
@@ -243,7 +398,15 @@ void launch_size(const Group<T>& g, int pass, cudaStream_t st) {
   switch (pass) {
     case 0: launch_pass<T, N1, N2, 0>(g, st); break;
     case 1: launch_pass<T, N1, N2, 1>(g, st); break;
-    case 2: launch_pass<T, N1, N2, 2>(g, st); break;
+    case 2:
+      if constexpr (sizeof(T) == 4 && zt_has<N1, N2>()) {
+        if (g.zt_grid > 0 && g.d_tmz) {
+          launch_zt<N1, N2>(g, st);
+          break;
+        }
+      }
+      launch_pass<T, N1, N2, 2>(g, st);
+      break;
     case 3: launch_pass<T, N1, N2, 3>(g, st); break;
     default: launch_pass<T, N1, N2, 4>(g, st); break;
   }
@@ -292,6 +455,50 @@ bool reg_plane_launch(const Group<T>& g, int dir, cudaStream_t st) {
     TTSH_FFTREG_SIZES(X)
 #undef X
     default: return false;
+  }
+}
+
+// The descriptor of one droplet's complex field for the staged z pass: 3-D, x in FP32 words
+// (2N, re/im interleaved), y, z; the box is LB lines x 1 row x N / NBOX planes.
+template <int N1, int N2>
+void zt_encode(const void* W, CUtensorMap* map) {
+  if constexpr (zt_has<N1, N2>()) {
+    constexpr int N = N1 * N2, LB = lines_per_cta<N>(), NBOX = (N + 255) / 256;
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+      void* fn = nullptr;
+      cudaDriverEntryPointQueryResult q{};
+      if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+          q != cudaDriverEntryPointSuccess || !fn)
+        throw std::runtime_error("cuTensorMapEncodeTiled is not available from the driver");
+      encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const cuuint64_t dims[3] = {2ull * N, (cuuint64_t)N, (cuuint64_t)N};
+    const cuuint64_t strides[2] = {2ull * N * sizeof(float), 2ull * N * N * sizeof(float)};
+    const cuuint32_t box[3] = {2u * LB, 1u, (cuuint32_t)(N / NBOX)};
+    const cuuint32_t es[3] = {1u, 1u, 1u};
+    const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(W), dims, strides, box, es,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  }
+}
+
+inline void reg_zt_encode(int N, const void* W, CUtensorMap* map) {
+  switch (N) {
+#define X(n, a, b) case n: zt_encode<a, b>(W, map); break;
+    TTSH_FFTREG_SIZES(X)
+#undef X
+    default: break;
+  }
+}
+
+inline int reg_zt_prepare(int N) {
+  switch (N) {
+#define X(n, a, b) case n: return zt_prepare<a, b>();
+    TTSH_FFTREG_SIZES(X)
+#undef X
+    default: return 0;
   }
 }
 

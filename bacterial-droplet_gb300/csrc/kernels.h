@@ -20,6 +20,11 @@ struct Group {
   int zc[3] = {64, 64, 64};  // z-planes per CTA of fused_rhs, fused_div, fused_correct
   double tuned_ms[4] = {0, 0, 0, 0};  // the tuner's timings of this configuration (host record)
   double* red = nullptr;  // FP64 diagnostics partials of the whole group (n x 4 x blocks), contiguous
+  // FP32 z pass staged by the tensor memory accelerator: a 3-D descriptor of each droplet's
+  // complex field (device array of n CUtensorMap) and the persistent grid (0: not used)
+  void* d_tmz = nullptr;
+  int zt_grid = 0;
+  int* d_err = nullptr;  // set to 1 by a kernel whose bounded wait for its input ran out
 };
 
 // Plain form (one thread per site, reference arithmetic order), plain.cu.
@@ -47,6 +52,9 @@ template <class T> bool fftreg_has(int N);
 // Forward x + y (dir 0) or inverse y + x (dir 1) of every z-plane, one CTA per plane (fft_kind 2):
 // false when the group does not use it.
 template <class T> bool fftreg_plane_launch(const Group<T>& g, int dir, cudaStream_t st);
+// The staged z pass of size N (FP32): builds the descriptors of the complex fields W[i] in a new
+// device array (*d_maps, caller frees) and returns the persistent grid; 0 when N has none.
+int fftreg_zt_setup(int N, const std::vector<const void*>& W, void** d_maps);
 
 // Fused FP32 form (fused.cu): rhs (u*, P*, phi'), div (packed Poisson source), correct (u, P).
 void launch_fused_rhs(const Group<float>& g, int par, cudaStream_t st);
