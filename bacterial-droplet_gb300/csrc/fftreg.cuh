@@ -25,6 +25,16 @@ template <class C>
 __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
 template <class C>
 __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+// FP32: one packed instruction (add/sub .f32x2: two IEEE FP32 operations, round to nearest, the
+// results of the two scalar ones) per complex add or subtract.
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+  float2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;"
+      : "=l"(*reinterpret_cast<unsigned long long*>(&d))
+      : "l"(*reinterpret_cast<const unsigned long long*>(&a)), "l"(*reinterpret_cast<const unsigned long long*>(&b)));
+  return d;
+}
 // exp(-+2 pi i k / N) from the table; conjugate for the inverse.
 template <class C, bool INV>
 __device__ __forceinline__ C tw(const C* t, int k) {
