@@ -258,10 +258,14 @@ constexpr size_t zt_smem() {
 }
 template <int N>
 constexpr int zt_min_blocks() { return 2 * zt_smem<N>() <= 227 * 1024 ? 2 : 1; }
-// The sizes with the staged z pass: a CTA of at least 128 threads, one or two boxes per line.
+// The sizes with the staged z pass: CTAs of 256 threads, two per SM (N = 256). Elsewhere the
+// directly loading kernel is faster and is kept, per step (ms, CUDA events): 64 x 128^3 0.573
+// against 0.644 staged (128-thread CTAs: a quarter of the direct kernel's resident warps); 512^3
+// 0.84 against 0.98 (240 registers a thread, one CTA per SM). At 2 x 256^3 they are level.
 template <int N1, int N2>
 constexpr bool zt_has() {
-  return lines_per_cta<N1 * N2>() == 16 && N2 >= 8 && (N1 * N2 <= 256 || N1 * N2 == 512) && zt_smem<N1 * N2>() <= 227 * 1024;
+  return lines_per_cta<N1 * N2>() == 16 && lines_per_cta<N1 * N2>() * N2 == 256 && N1 * N2 <= 256 &&
+         zt_min_blocks<N1 * N2>() == 2;
 }
 
 template <int N1, int N2>

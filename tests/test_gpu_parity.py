@@ -184,10 +184,11 @@ def test_plane_fft_matches_separate_passes_fp32(N, monkeypatch):
         assert np.array_equal(runs["separate"][k], runs[None][k]), k
 
 
-@pytest.mark.parametrize("N,fft", [(64, None), (128, "separate"), (256, None), (512, None)])
-def test_staged_z_pass_matches_direct_loads(N, fft, monkeypatch):
-    """FP32: the z pass whose input the tensor memory accelerator stages in shared memory gives the
-    same bits as the z pass that loads its input directly (TTSH_ZTMA=0)."""
+@pytest.mark.parametrize("fft", [None, "separate"])
+def test_staged_z_pass_matches_direct_loads(fft, monkeypatch):
+    """FP32, 256^3: the z pass whose input the tensor memory accelerator stages in shared memory
+    gives the same bits as the z pass that loads its input directly (TTSH_ZTMA=0)."""
+    N = 256
     st = random_state(N, seed=N + 9)
     if fft:
         monkeypatch.setenv("TTSH_FFT", fft)
@@ -197,7 +198,7 @@ def test_staged_z_pass_matches_direct_loads(N, fft, monkeypatch):
             monkeypatch.delenv("TTSH_ZTMA", raising=False)
         else:
             monkeypatch.setenv("TTSH_ZTMA", zt)
-        runs[zt] = run_gpu(st, 2 if N < 512 else 1, 32, 0, 1, 0.02)
+        runs[zt] = run_gpu(st, 2, 32, 0, 1, 0.02)
     monkeypatch.delenv("TTSH_ZTMA", raising=False)
     monkeypatch.delenv("TTSH_FFT", raising=False)
     for k in FIELDS:
