@@ -555,7 +555,8 @@ std::string check_tuning(const ttsh_sim* s, const Group<T>& G, const ttsh_tuning
   if (prod != G.N) return "tuning: radix plan does not multiply to N";
   if (s->fused)
     for (int k = 0; k < 3; ++k) {
-      if (t.zc[k] < 1) return "tuning: z-planes per CTA must be >= 1";
+      if (t.zc[k] == 0) continue;  // the persistent grid
+      if (t.zc[k] < 1) return "tuning: z-planes per CTA must be >= 1, or 0 (persistent grid)";
       if ((long)((G.N + t.zc[k] - 1) / t.zc[k]) * G.n > 65535) return "tuning: grid too large";
     }
   return "";
@@ -653,13 +654,14 @@ void tune_group(ttsh_sim* s, Engine<T>& E, size_t gi, ttsh_tuning* out) {
     set_radix(s, E, gi, pick.radix);
     double ms[4] = {best, 0, 0, 0};
     if (s->fused) {
-      const int zcs[] = {8, 16, 32, 64, 128, 256};
+      // z-planes per CTA; 0: the persistent grid (equal shares of the group's sites per CTA)
+      const int zcs[] = {0, 8, 16, 32, 64, 128, 256};
       for (int k = 0; k < 3; ++k) {
         double bk_t = 1e30;
         int bk_z = G.zc[k];
         for (int z : zcs) {
-          if (z > G.N && z != zcs[0]) continue;
-          if ((long)((G.N + z - 1) / z) * G.n > 65535) continue;
+          if (z > G.N && z != zcs[1]) continue;
+          if (z > 0 && (long)((G.N + z - 1) / z) * G.n > 65535) continue;
           G.zc[k] = z;
           const double t = time_graph(st, reps, [] {}, [&] {
             if (k == 0) E.launch_fused_rhs_t(G, par, st);

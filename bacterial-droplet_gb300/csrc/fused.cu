@@ -28,8 +28,10 @@
 // st_lap of common.cuh, TTSH3D.cu:3280-3343) in FP32, regrouped separably; the stress enters as
 // one field per component, S_ab = cA phi D_a P_b - zeta phi P_a P_b, whose divergence is the
 // reference's cA * div(sigma) plus the build-defined active stress.
+#include <algorithm>
 #include <cstdio>
 #include <stdexcept>
+#include <utility>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -160,15 +162,11 @@ __device__ __forceinline__ void sep_rows(const LD& ld, const SepK& k, V* dx, V* 
 }
 
 // ------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc) {
-  extern __shared__ __align__(16) unsigned char smr[];
-  const int N = insts[0].N;
-  const InstDev<float>& I = insts[blockIdx.z / nchunk];
+// One segment of the sweep: the tile column (x0, y0) of droplet I, output planes z0 .. z1 - 1.
+__device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, int N, int x0, int y0, int z0, int z1,
+                                            unsigned char* smr) {
   const Phys<float> p = I.ph;  // by value: read once, kept in registers
   const SepK sk{p.c2h * (1.f / 36.f), p.cl12, p.cl23, p.cl143};
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-  const int z0 = (blockIdx.z % nchunk) * zc;  // zc z-planes per block (a tuning choice)
-  const int z1 = min(z0 + zc, N);
   const size_t NN = (size_t)N * N;
   const float* __restrict__ gphi = I.phi[par];
   const float* __restrict__ gP[3] = {I.P[0], I.P[1], I.P[2]};
@@ -529,6 +527,45 @@ __global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __res
   }
 }
 
+// The two schedules of the three fused kernels. zc > 0: CTA (bx, by, bz) sweeps tile (bx, by)
+// (TW x TH columns) of droplet bz / nchunk over the zc planes of chunk bz % nchunk. zc == 0: a
+// persistent grid (as many CTAs as fit on the device at once); the output sites of all droplets,
+// in the order (droplet, tile row, tile column, plane), are split into gridDim.x equal contiguous
+// shares, each swept as one segment per tile column it touches, so that no SM waits out a last
+// partial wave of CTAs. seg(inst, x0, y0, z0, z1) sweeps one segment. Each kernel is built for
+// both (PERSIST), so that the chunked form carries no loop state.
+template <int TW, int TH, bool PERSIST, class F>
+__device__ __forceinline__ void sweep_schedule(int N, int nchunk, int zc, int ninst, F&& seg) {
+  if constexpr (!PERSIST) {
+    const int z0 = (blockIdx.z % nchunk) * zc;
+    seg((int)(blockIdx.z / nchunk), (int)blockIdx.x * TW, (int)blockIdx.y * TH, z0, min(z0 + zc, N));
+    return;
+  }
+  const int TXN = N / TW, TPI = TXN * (N / TH);  // tile columns per row, per droplet
+  const long long total = (long long)ninst * TPI * N;
+  long long w = (long long)blockIdx.x * total / gridDim.x;
+  const long long w1 = (long long)(blockIdx.x + 1) * total / gridDim.x;
+  while (w < w1) {
+    const long long col = w / N;
+    const int z0 = (int)(w - col * N);
+    const int z1 = (int)min((long long)N, z0 + (w1 - w));
+    const int inst = (int)(col / TPI), t = (int)(col - (long long)inst * TPI);
+    seg(inst, (t % TXN) * TW, (t / TXN) * TH, z0, z1);
+    __syncthreads();  // the next segment refills the rings the last one read
+    w += z1 - z0;
+  }
+}
+
+template <bool PERSIST>
+__global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc,
+                                                     int ninst) {
+  extern __shared__ __align__(16) unsigned char smr[];
+  const int N = insts[0].N;
+  sweep_schedule<TX, TY, PERSIST>(N, nchunk, zc, ninst, [&](int inst, int x0, int y0, int z0, int z1) {
+    rhs_segment(insts[inst], par, N, x0, y0, z0, z1, smr);
+  });
+}
+
 // ------------------------------------------------------------------------------------------
 // fused_div / fused_correct: one tile column per thread; each staged plane is read once, its
 // in-plane partial sums carried in z (as in fused_rhs phase 2), so the ring only has to cover
@@ -566,12 +603,8 @@ __device__ __forceinline__ void cp_async_wait_div() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(DRD - 2) : "memory");
 }
 
-__global__ void __launch_bounds__(NTV, 2) k_fused_div(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc) {
-  extern __shared__ __align__(16) float sm[];
-  const int N = insts[0].N;
-  const InstDev<float>& I = insts[blockIdx.z / nchunk];
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TYD;
-  const int z0 = (blockIdx.z % nchunk) * zc, z1 = min(z0 + zc, N);
+__device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, int N, int x0, int y0, int z0, int z1,
+                                            float* sm) {
   const size_t NN = (size_t)N * N;
   const float* cur[6] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2],
                          I.Ps[par ^ 1][0], I.Ps[par ^ 1][1], I.Ps[par ^ 1][2]};
@@ -641,14 +674,20 @@ __global__ void __launch_bounds__(NTV, 2) k_fused_div(const InstDev<float>* __re
   }
 }
 
-__global__ void __launch_bounds__(NTC, 2) k_fused_correct(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc) {
-  extern __shared__ __align__(16) unsigned char smc[];
+template <bool PERSIST>
+__global__ void __launch_bounds__(NTV, 2) k_fused_div(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc,
+                                                       int ninst) {
+  extern __shared__ __align__(16) float sm[];
   const int N = insts[0].N;
-  const InstDev<float>& I = insts[blockIdx.z / nchunk];
+  sweep_schedule<TX, TYD, PERSIST>(N, nchunk, zc, ninst, [&](int inst, int x0, int y0, int z0, int z1) {
+    div_segment(insts[inst], par, N, x0, y0, z0, z1, sm);
+  });
+}
+
+__device__ __forceinline__ void correct_segment(const InstDev<float>& I, int par, int N, int x0, int y0, int z0, int z1,
+                                                unsigned char* smc) {
   const float kd = I.ph.c2h * (1.f / 36.f);
   const float dt = I.ph.dt;
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-  const int z0 = (blockIdx.z % nchunk) * zc, z1 = min(z0 + zc, N);
   const size_t NN = (size_t)N * N;
   const int niter = (z1 - z0) + 2;
   const float* qs[6] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2],
@@ -733,6 +772,16 @@ __global__ void __launch_bounds__(NTC, 2) k_fused_correct(const InstDev<float>* 
   }
 }
 
+template <bool PERSIST>
+__global__ void __launch_bounds__(NTC, 2) k_fused_correct(const InstDev<float>* __restrict__ insts, int par, int nchunk,
+                                                          int zc, int ninst) {
+  extern __shared__ __align__(16) unsigned char smc[];
+  const int N = insts[0].N;
+  sweep_schedule<TX, TY, PERSIST>(N, nchunk, zc, ninst, [&](int inst, int x0, int y0, int z0, int z1) {
+    correct_segment(insts[inst], par, N, x0, y0, z0, z1, smc);
+  });
+}
+
 inline void check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
 }
@@ -749,34 +798,58 @@ dim3 grid_for(const Group<float>& g, int zc, int& nchunk) {
 bool fused_supported(int N) { return N >= 32 && N % TX == 0 && N % TY == 0 && N % TYD == 0; }
 
 void fused_prepare() {
-  check(cudaFuncSetAttribute(k_fused_rhs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RHS_SMEM),
-        "fused_rhs smem attribute");
-  check(cudaFuncSetAttribute(k_fused_div, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DIV_SMEM),
-        "fused_div smem attribute");
-  check(cudaFuncSetAttribute(k_fused_correct, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)COR_SMEM),
-        "fused_correct smem attribute");
+  const std::pair<const void*, size_t> k[] = {
+      {(const void*)k_fused_rhs<false>, RHS_SMEM},     {(const void*)k_fused_rhs<true>, RHS_SMEM},
+      {(const void*)k_fused_div<false>, DIV_SMEM},     {(const void*)k_fused_div<true>, DIV_SMEM},
+      {(const void*)k_fused_correct<false>, COR_SMEM}, {(const void*)k_fused_correct<true>, COR_SMEM}};
+  for (const auto& f : k)
+    check(cudaFuncSetAttribute(f.first, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f.second),
+          "fused kernels' smem attribute");
+}
+
+// The persistent grid of a fused kernel (zc == 0): the CTAs that fit on the device at once, at
+// most one per plane of a tile column.
+static int persistent_grid(const void* kernel, int threads, size_t smem, long long planes, int* cache) {
+  if (!*cache) {
+    int dev = 0, sms = 0, per = 0;
+    check(cudaGetDevice(&dev), "fused: device");
+    check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "fused: SM count");
+    check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, smem), "fused: occupancy");
+    if (per < 1) throw std::runtime_error("fused: kernel does not fit on an SM");
+    *cache = sms * per;
+  }
+  return (int)std::min<long long>(*cache, planes);
+}
+
+template <class K>
+static void launch_sweep(K chunked, K persistent, const Group<float>& g, int par, int zc, int th, int threads, size_t smem,
+                         int* cache, cudaStream_t st, const char* what) {
+  if (zc == 0) {
+    const long long planes = (long long)g.n * (g.N / TX) * (g.N / th) * g.N;
+    const int grid = persistent_grid((const void*)persistent, threads, smem, planes, cache);
+    persistent<<<grid, threads, smem, st>>>(g.d_inst, par, 1, 0, g.n);
+  } else {
+    int nchunk;
+    dim3 grid = grid_for(g, zc, nchunk);
+    grid.y = g.N / th;
+    chunked<<<grid, threads, smem, st>>>(g.d_inst, par, nchunk, zc, g.n);
+  }
+  check(cudaGetLastError(), what);
 }
 
 void launch_fused_rhs(const Group<float>& g, int par, cudaStream_t st) {
-  int nchunk;
-  dim3 grid = grid_for(g, g.zc[0], nchunk);
-  k_fused_rhs<<<grid, NT, RHS_SMEM, st>>>(g.d_inst, par, nchunk, g.zc[0]);
-  check(cudaGetLastError(), "fused_rhs launch");
+  static int cache = 0;
+  launch_sweep(k_fused_rhs<false>, k_fused_rhs<true>, g, par, g.zc[0], TY, NT, RHS_SMEM, &cache, st, "fused_rhs launch");
 }
 
 void launch_fused_div(const Group<float>& g, int par, cudaStream_t st) {
-  int nchunk;
-  dim3 grid = grid_for(g, g.zc[1], nchunk);
-  grid.y = g.N / TYD;
-  k_fused_div<<<grid, NTV, DIV_SMEM, st>>>(g.d_inst, par, nchunk, g.zc[1]);
-  check(cudaGetLastError(), "fused_div launch");
+  static int cache = 0;
+  launch_sweep(k_fused_div<false>, k_fused_div<true>, g, par, g.zc[1], TYD, NTV, DIV_SMEM, &cache, st, "fused_div launch");
 }
 
 void launch_fused_correct(const Group<float>& g, int par, cudaStream_t st) {
-  int nchunk;
-  dim3 grid = grid_for(g, g.zc[2], nchunk);
-  k_fused_correct<<<grid, NTC, COR_SMEM, st>>>(g.d_inst, par, nchunk, g.zc[2]);
-  check(cudaGetLastError(), "fused_correct launch");
+  static int cache = 0;
+  launch_sweep(k_fused_correct<false>, k_fused_correct<true>, g, par, g.zc[2], TY, NTC, COR_SMEM, &cache, st, "fused_correct launch");
 }
 
 }  // namespace ttsh

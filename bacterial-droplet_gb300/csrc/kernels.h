@@ -17,7 +17,8 @@ struct Group {
   int fft_kind = 0;    // register-resident FFT kernels where the size has them: 0 one launch per
                        // axis pass, 2 x and y of a plane in one launch; 1: Stockham only
   int fft_lb = 0;      // Stockham lines per CTA (0: the largest power of two that fits)
-  int zc[3] = {64, 64, 64};  // z-planes per CTA of fused_rhs, fused_div, fused_correct
+  int zc[3] = {0, 64, 64};   // z-planes per CTA of fused_rhs, fused_div, fused_correct; 0: the
+                             // persistent grid (equal shares of the group's sites per CTA)
   double tuned_ms[4] = {0, 0, 0, 0};  // the tuner's timings of this configuration (host record)
   double* red = nullptr;  // FP64 diagnostics partials of the whole group (n x 4 x blocks), contiguous
   // FP32 z pass staged by the tensor memory accelerator: a 3-D descriptor of each droplet's

@@ -231,7 +231,9 @@ typedef struct {
   int fft_lb;      /* Stockham lines per CTA; 0 = the largest that fits */
   int nstages;     /* Stockham radix plan: radix[0..nstages-1], each 2, 3, 4 or 5, product N */
   int radix[16];
-  int zc[3];       /* z-planes per CTA of fused_rhs, fused_div, fused_correct (fused form) */
+  int zc[3];       /* z-planes per CTA of fused_rhs, fused_div, fused_correct (fused form);
+                      0: a persistent grid (the CTAs that fit on the device at once), each CTA
+                      sweeping an equal contiguous share of the group's (droplet, tile, plane) sites */
   double ms[4];    /* measured per launch: FFT (5 passes), fused_rhs, fused_div, fused_correct;
                       0 where not measured (taken from a cache, or set by the caller) */
 } ttsh_tuning;
