@@ -40,20 +40,21 @@ namespace ttsh {
 
 namespace {
 
-constexpr int TX = 32, TY = 16;   // output tile (columns)
-constexpr int RB = 3;             // strip length (sites per thread) of fused_rhs stage 1 (a 5-row window)
-constexpr int NT = 512;           // threads of fused_rhs: one tile column each in phase 2
+constexpr int TX = 32, TY = 16;   // output tile (columns) of fused_correct
+constexpr int TYR = 8;            // fused_rhs: tiles of TX x TYR columns, two CTAs per SM
+constexpr int RB = 2;             // strip length (sites per thread) of fused_rhs stage 1 (a 4-row window)
+constexpr int NT = TX * TYR;      // threads of fused_rhs: one tile column each in phase 2
 constexpr int US = 4;             // strip length of the velocity terms (phase 1)
 
 // fused_rhs regions: A = tile + 2 (phi, P), B = tile + 1 (u, stage-1 products), C = tile.
-constexpr int AW = TX + 4, AH = TY + 4, AN = AW * AH;
-constexpr int BW = TX + 2, BH = TY + 2, BN = BW * BH;
-constexpr int CN = TX * TY;
+constexpr int AW = TX + 4, AH = TYR + 4, AN = AW * AH;
+constexpr int BW = TX + 2, BH = TYR + 2, BN = BW * BH;
+constexpr int CN = TX * TY;  // fused_correct's tile
 // Row pitches in shared memory, one element longer than the rows: warps whose lanes sit in
 // different rows (the stage-1 strips of the last two B columns) then hit different banks.
 constexpr int AP = AW + 1, ANP = AP * AH;  // A region (float2 pairs)
 constexpr int BP = BW + 1, BNP = BP * BH;  // B region
-constexpr int CP = TX + 1, CNP = CP * TY;  // the tile (partials)
+constexpr int CP = TX + 1, CNP = CP * TYR;  // the tile (partials)
 // Products of one plane on B, as float2 pairs (plus one scalar field):
 //   M0 = (mu_0, mu_x), M1 = (mu_y, mu_z)       Laplacians: phi', P*
 //   T0 = (S_xy, S_xz), T1 = (S_yy, S_yz), T2 = (S_zy, S_zz)   divergence columns y, z
@@ -73,13 +74,14 @@ constexpr size_t OFF_PR = OFF_U2 + (((size_t)RU * BNP * sizeof(float) + 15) / 16
 constexpr size_t OFF_SZX = OFF_PR + (size_t)NPR * BNP * sizeof(float2);
 constexpr size_t OFF_PQ = OFF_SZX + (((size_t)BNP * sizeof(float) + 15) / 16) * 16;
 constexpr size_t RHS_SMEM = OFF_PQ + (size_t)2 * NPQ * CNP * sizeof(float2);
+static_assert(2 * RHS_SMEM <= 227 * 1024, "fused_rhs: two CTAs per SM");
 static_assert(OFF_U01 % 16 == 0 && OFF_U2 % 16 == 0 && OFF_PR % 16 == 0 && OFF_SZX % 16 == 0 && OFF_PQ % 16 == 0,
               "16-byte aligned regions");
 // phase-1 thread roles of fused_rhs: stage-1 strips of the B region, then the velocity strips
 constexpr int NS1 = (BW * BH) / RB;                   // 204 stage-1 strips
 constexpr int NU0 = ((NS1 + 31) / 32) * 32;           // first velocity thread (warp aligned)
-constexpr int NUS = TX * (TY / US);                   // 128 velocity strips
-static_assert((BH % RB) == 0 && (TY % US) == 0, "strip lengths divide the regions");
+constexpr int NUS = TX * (TYR / US);                  // velocity strips
+static_assert((BH % RB) == 0 && (TYR % US) == 0, "strip lengths divide the regions");
 static_assert(NU0 + NUS <= NT, "phase-1 roles fit the block");
 
 __device__ __forceinline__ int wrapN(int a, int N) { return a < 0 ? a + N : (a >= N ? a - N : a); }
@@ -240,7 +242,7 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
   // (mu_y, mu_z) and the divergence of stress column x, then P*, phi' and u*_x; half B the
   // divergence of stress columns (y, z), then u*_y, u*_z. Each half has every input of what it
   // writes. The sites' rows share a 4 x 3 window of each product plane.
-  static_assert(NT == 2 * TX * (TY / 2), "phase 2: two halves of 2-site strips");
+  static_assert(NT == 2 * TX * (TYR / 2), "phase 2: two halves of 2-site strips");
   const bool halfA = tid < NT / 2;
   const int ps = tid & (NT / 2 - 1);
   const int px = ps % TX, py0 = (ps / TX) * 2;
@@ -322,7 +324,7 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
         sPr[PT3 * BNP + o] = f2(sx[0], sx[1]);
         sSzx[o] = sx[2];
         const int cx = bx - 1, cy = by0 + k - 1;
-        if (cx >= 0 && cx < TX && cy >= 0 && cy < TY) {
+        if (cx >= 0 && cx < TX && cy >= 0 && cy < TYR) {
           // pointwise parts of getDtF (:617-631) at this site of plane b:
           //   u_b:  mu_0 D_b phi;  phi: -u.D phi;
           //   P_b:  -(u + lambda0 P).D P_b - P_b (alpha phi + beta |P|^2 + A |D phi|^2 |P|^2)
@@ -557,11 +559,11 @@ __device__ __forceinline__ void sweep_schedule(int N, int nchunk, int zc, int ni
 }
 
 template <bool PERSIST>
-__global__ void __launch_bounds__(NT, 1) k_fused_rhs(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc,
+__global__ void __launch_bounds__(NT, 2) k_fused_rhs(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc,
                                                      int ninst) {
   extern __shared__ __align__(16) unsigned char smr[];
   const int N = insts[0].N;
-  sweep_schedule<TX, TY, PERSIST>(N, nchunk, zc, ninst, [&](int inst, int x0, int y0, int z0, int z1) {
+  sweep_schedule<TX, TYR, PERSIST>(N, nchunk, zc, ninst, [&](int inst, int x0, int y0, int z0, int z1) {
     rhs_segment(insts[inst], par, N, x0, y0, z0, z1, smr);
   });
 }
@@ -839,7 +841,7 @@ static void launch_sweep(K chunked, K persistent, const Group<float>& g, int par
 
 void launch_fused_rhs(const Group<float>& g, int par, cudaStream_t st) {
   static int cache = 0;
-  launch_sweep(k_fused_rhs<false>, k_fused_rhs<true>, g, par, g.zc[0], TY, NT, RHS_SMEM, &cache, st, "fused_rhs launch");
+  launch_sweep(k_fused_rhs<false>, k_fused_rhs<true>, g, par, g.zc[0], TYR, NT, RHS_SMEM, &cache, st, "fused_rhs launch");
 }
 
 void launch_fused_div(const Group<float>& g, int par, cudaStream_t st) {
