@@ -531,11 +531,13 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
 
 // The two schedules of the three fused kernels. zc > 0: CTA (bx, by, bz) sweeps tile (bx, by)
 // (TW x TH columns) of droplet bz / nchunk over the zc planes of chunk bz % nchunk. zc == 0: a
-// persistent grid (as many CTAs as fit on the device at once); the output sites of all droplets,
-// in the order (droplet, tile row, tile column, plane), are split into gridDim.x equal contiguous
-// shares, each swept as one segment per tile column it touches, so that no SM waits out a last
-// partial wave of CTAs. seg(inst, x0, y0, z0, z1) sweeps one segment. Each kernel is built for
-// both (PERSIST), so that the chunked form carries no loop state.
+// persistent grid of G CTAs (as many as fit on the device at once) over the items (droplet, slab
+// of S planes, tile row, tile column): in rounds, CTA b sweeps items b, b + G, b + 2G, ... while
+// every CTA has a whole one (so the CTAs running at the same time hold neighbouring tiles of one
+// slab and meet each other's halo planes in L2, as a chunked grid does); the items left over
+// are then split into G equal contiguous runs of planes, so that no SM waits out a last partial
+// wave. seg(inst, x0, y0, z0, z1) sweeps one segment. Each kernel is built for both (PERSIST),
+// so that the chunked form carries no loop state.
 template <int TW, int TH, bool PERSIST, class F>
 __device__ __forceinline__ void sweep_schedule(int N, int nchunk, int zc, int ninst, F&& seg) {
   if constexpr (!PERSIST) {
@@ -544,17 +546,34 @@ __device__ __forceinline__ void sweep_schedule(int N, int nchunk, int zc, int ni
     return;
   }
   const int TXN = N / TW, TPI = TXN * (N / TH);  // tile columns per row, per droplet
-  const long long total = (long long)ninst * TPI * N;
-  long long w = (long long)blockIdx.x * total / gridDim.x;
-  const long long w1 = (long long)(blockIdx.x + 1) * total / gridDim.x;
-  while (w < w1) {
-    const long long col = w / N;
-    const int z0 = (int)(w - col * N);
-    const int z1 = (int)min((long long)N, z0 + (w1 - w));
-    const int inst = (int)(col / TPI), t = (int)(col - (long long)inst * TPI);
-    seg(inst, (t % TXN) * TW, (t / TXN) * TH, z0, z1);
+  int S = N;                                     // slab height: a divisor of N, at most 128 where N allows
+  while (S > 128 && S % 2 == 0) S /= 2;
+  const int NS = N / S;
+  const int items = ninst * NS * TPI, G = gridDim.x;
+  const int full = items / G;
+  const long long rest = (long long)(items - full * G) * S;  // planes of the items left over
+  long long w = (long long)blockIdx.x * rest / G;
+  const long long w1 = (long long)(blockIdx.x + 1) * rest / G;
+  int k = 0;
+  for (;;) {  // one call site of seg: the rounds, then this CTA's run of the rest
+    int item, za, zb;
+    if (k < full) {
+      item = k++ * G + (int)blockIdx.x;
+      za = 0;
+      zb = S;
+    } else if (w < w1) {
+      const int q = (int)(w / S);
+      za = (int)(w - (long long)q * S);
+      zb = (int)min((long long)S, za + (w1 - w));
+      item = full * G + q;
+      w += zb - za;
+    } else {
+      break;
+    }
+    const int inst = item / (NS * TPI), r = item - inst * NS * TPI;
+    const int sl = r / TPI, t = r - sl * TPI;
+    seg(inst, (t % TXN) * TW, (t / TXN) * TH, sl * S + za, sl * S + zb);
     __syncthreads();  // the next segment refills the rings the last one read
-    w += z1 - z0;
   }
 }
 

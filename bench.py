@@ -60,10 +60,10 @@ KERNEL_WORDS = {
 }
 
 # DRAM bytes per site of the dominant FP32 kernels, dram__bytes_read.sum + dram__bytes_write.sum
-# of one ncu capture on a 256^3 droplet (--set full, --clock-control none); a launch over more
-# sites scales with the sites (every kernel streams its planes once).
+# of one ncu capture of the default configuration on a 256^3 droplet (--clock-control none); a
+# launch over more sites scales with the sites (every kernel streams its planes once).
 TRAFFIC_BYTES_PER_SITE_F32 = {
-    "fused_rhs": (557.067264e6 + 493.400832e6) / 256 ** 3,
+    "fused_rhs": (905.68e6 + 512.09e6) / 256 ** 3,
 }
 
 
