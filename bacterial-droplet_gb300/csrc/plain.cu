@@ -208,33 +208,9 @@ struct MassAcc<float> {
   __device__ __forceinline__ double total() const { return (double)s - (double)c; }
 };
 
-template <class T, bool FULL>
-__global__ void __launch_bounds__(STATS_THREADS) k_stats(const InstDev<T>* __restrict__ insts, int par) {
-  const InstDev<T>& I = insts[blockIdx.y];
-  const int N = I.N;
-  const long n = (long)N * N * N;
-  const Phys<T>& p = I.ph;
-  const T* phi = I.phi[par];
-  MassAcc<T> acc;
-  T mdivT = 0, muT = 0;
-  int badn = 0;
-  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const T ph = phi[i];
-    acc.add(ph);
-    if (!isfinite(ph)) badn += 1;
-    if (!FULL) continue;
-    const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / ((long)N * N));
-    Site s;
-    s.init(x, y, z, N);
-    const T d = st_dx<T>(s.acc<T>(I.U[0]), p.c2h) + st_dy<T>(s.acc<T>(I.U[1]), p.c2h) + st_dz<T>(s.acc<T>(I.U[2]), p.c2h);
-    mdivT = fmax(mdivT, fabs(d));
-    for (int b = 0; b < 3; ++b) {
-      const T u = I.U[b][i], q = I.P[b][i];
-      muT = fmax(muT, fabs(u));
-      if (!isfinite(u) || !isfinite(q)) badn += 1;
-    }
-  }
-  double sum = acc.total(), mdiv = (double)mdivT, mu = (double)muT, bad = (double)badn;
+// Block reduction of the four per-thread diagnostics (fixed order) into the block's partials.
+template <class T>
+__device__ __forceinline__ void stats_finish(const InstDev<T>& I, double sum, double mdiv, double mu, double bad) {
   __shared__ double sh[4][STATS_THREADS / 32];
   for (int o = 16; o > 0; o >>= 1) {
     sum += __shfl_down_sync(0xffffffffu, sum, o);
@@ -253,6 +229,76 @@ __global__ void __launch_bounds__(STATS_THREADS) k_stats(const InstDev<T>* __res
     double* out = I.red + 4 * blockIdx.x;
     out[0] = a; out[1] = b; out[2] = c; out[3] = e;
   }
+}
+
+// 16-byte vectors of T (the mass-only pass reads phi with them).
+template <class T> struct Vec16;
+template <> struct Vec16<float> { typedef float4 type; };
+template <> struct Vec16<double> { typedef double2 type; };
+
+// Sum of phi over this thread's share of the sites (fixed order) and the count of non-finite
+// values: 16-byte loads, four in flight per thread, and one compensated accumulator per vector
+// lane, so that the pass streams phi at HBM speed (one 4-byte load per thread in flight had kept
+// it at a few hundred GB/s). Both diagnostics modes take the mass from here, so they agree.
+template <class T>
+__device__ __forceinline__ double mass_pass(const T* __restrict__ phi, long n, int& badn) {
+  typedef typename Vec16<T>::type V;
+  constexpr int W = (int)(sizeof(V) / sizeof(T));
+  const long nv = n / W, stride = (long)gridDim.x * blockDim.x;
+  const V* __restrict__ pv = reinterpret_cast<const V*>(phi);
+  MassAcc<T> lane[W];
+  auto take = [&](const V& v) {
+    const T* e = reinterpret_cast<const T*>(&v);
+#pragma unroll
+    for (int c = 0; c < W; ++c) {
+      lane[c].add(e[c]);
+      badn += isfinite(e[c]) ? 0 : 1;
+    }
+  };
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < nv; i += 4 * stride) {
+    V v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) v[u] = pv[i + u * stride];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) take(v[u]);
+  }
+  for (; i < nv; i += stride) take(pv[i]);
+  for (long j = nv * W + (long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+    lane[0].add(phi[j]);
+    badn += isfinite(phi[j]) ? 0 : 1;
+  }
+  double tot = 0;
+#pragma unroll
+  for (int c = 0; c < W; ++c) tot += lane[c].total();
+  return tot;
+}
+
+template <class T, bool FULL>
+__global__ void __launch_bounds__(STATS_THREADS) k_stats(const InstDev<T>* __restrict__ insts, int par) {
+  const InstDev<T>& I = insts[blockIdx.y];
+  const int N = I.N;
+  const long n = (long)N * N * N;
+  int badn = 0;
+  const double mass = mass_pass<T>(I.phi[par], n, badn);
+  T mdivT = 0, muT = 0;
+  if constexpr (FULL) {
+    // max |D.u|, max |u| and the non-finite values of u and P
+    const Phys<T>& p = I.ph;
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+      const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / ((long)N * N));
+      Site s;
+      s.init(x, y, z, N);
+      const T d = st_dx<T>(s.acc<T>(I.U[0]), p.c2h) + st_dy<T>(s.acc<T>(I.U[1]), p.c2h) + st_dz<T>(s.acc<T>(I.U[2]), p.c2h);
+      mdivT = fmax(mdivT, fabs(d));
+      for (int b = 0; b < 3; ++b) {
+        const T u = I.U[b][i], q = I.P[b][i];
+        muT = fmax(muT, fabs(u));
+        if (!isfinite(u) || !isfinite(q)) badn += 1;
+      }
+    }
+  }
+  stats_finish<T>(I, mass, (double)mdivT, (double)muT, (double)badn);
 }
 
 }  // namespace
