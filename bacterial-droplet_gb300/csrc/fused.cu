@@ -658,6 +658,11 @@ __device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, in
   const int qx = tid % TX, qy0 = (tid / TX) * USD;
   const size_t gc0 = (size_t)(y0 + qy0) * N + (x0 + qx);
   const int wbase = qy0 * SW + (qx + 3);  // staged index of window row 0 (site 0's row - 1), column x - 1
+  // column x sits at the even staged index qx + 4 (rows and planes have even lengths), so the
+  // aligned pair holding it starts at column offset pb of the window and the third column is sc
+  const bool odd = (qx & 1) != 0;
+  const int pb = odd ? 0 : 1, sc = odd ? 2 : 0;
+  static_assert(SW % 2 == 0 && SPLD % 2 == 0, "aligned column pairs in the staged rows");
   // the divergence D_x v_x + D_y v_y + D_z v_z of v = (u*, P*) (getStream mode 0, :664-670), each
   // D = d/36 delta s s: a plane adds Q = delta_x s_y v_x + s_x delta_y v_y with weight s_z =
   // (1, 4, 1) and Z = s_x s_y v_z with weight delta_z = (-1, 0, 1) over planes c-1, c, c+1
@@ -673,13 +678,28 @@ __device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, in
     issue(i + DRD - 1);  // into the slot read at iteration i - 1
     const float* s = sm + (i % DRD) * 6 * SPLD + wbase;
     auto w = [&](int comp, int r, int c) { return f2(s[comp * SPLD + r * SW + c], s[(3 + comp) * SPLD + r * SW + c]); };
+    // the three columns x - 1, x, x + 1 of field f in window row r with two loads: the aligned
+    // pair that holds x (x - 1, x for odd x; x, x + 1 for even x) and the remaining column
+    auto row3 = [&](int f, int r, float& c0, float& c1, float& c2) {
+      const float* q = s + f * SPLD + r * SW;
+      const float2 pr = *reinterpret_cast<const float2*>(q + pb);
+      const float sv = q[sc];
+      c0 = odd ? pr.x : sv;
+      c1 = odd ? pr.y : pr.x;
+      c2 = odd ? sv : pr.y;
+    };
     // per row of the window: the x-part delta_x v_x, and s_x of v_y and of v_z
     float2 xd[USD + 2], ys[USD + 2], zs[USD + 2];
 #pragma unroll
     for (int r = 0; r < USD + 2; ++r) {
       xd[r] = vsub(w(0, r, 2), w(0, r, 0));
-      ys[r] = vfma(four, w(1, r, 1), vadd(w(1, r, 0), w(1, r, 2)));
-      zs[r] = vfma(four, w(2, r, 1), vadd(w(2, r, 0), w(2, r, 2)));
+      float a0, a1, a2, b0, b1, b2;
+      row3(1, r, a0, a1, a2);
+      row3(4, r, b0, b1, b2);
+      ys[r] = vfma(four, f2(a1, b1), vadd(f2(a0, b0), f2(a2, b2)));
+      row3(2, r, a0, a1, a2);
+      row3(5, r, b0, b1, b2);
+      zs[r] = vfma(four, f2(a1, b1), vadd(f2(a0, b0), f2(a2, b2)));
     }
 #pragma unroll
     for (int k = 0; k < USD; ++k) {
