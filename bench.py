@@ -336,6 +336,8 @@ def main():
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
+        esampler = ClockSampler(local)
+        esampler.start()
         t0 = time.perf_counter()
         for i, (phi, P, u, _) in enumerate(pin):
             sim.set_state(i, phi, P, u)
@@ -349,6 +351,7 @@ def main():
             ttsh._check(lib_rc)
         torch.cuda.synchronize()
         t3 = time.perf_counter()
+        eclocks = esampler.stop()
         last = sim.stats_from_partials(diag[args.steps - 1], check=False)
         assert last[0]["steps"] == diag[0, 0] + args.steps - 1 and all(d["nonfinite"] == 0 for d in last)
         wall = replicas.max_over_ranks(t3 - t0, device="cuda")
@@ -360,7 +363,8 @@ def main():
                "note": "public API (ttsh.Sim): set_state from pinned host FP64 arrays, %d x (step + FP64 "
                        "mass diagnostics of every droplet, ttsh_reduce_all_async into pinned host rows, read after the "
                        "final sync), get_state of all fields into "
-                       "pinned host FP64 arrays; wall clock" % args.steps, "split": split}
+                       "pinned host FP64 arrays; wall clock" % args.steps, "split": split,
+               "clocks": eclocks}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
