@@ -277,8 +277,8 @@ __global__ void __launch_bounds__(lines_per_cta<N1 * N2>() * N2, zt_min_blocks<N
   constexpr int NBOX = (N + 255) / 256, BZ = N / NBOX;
   static_assert(NBOX * BZ == N, "the boxes tile a line");
   constexpr unsigned STAGE = (unsigned)(N * LB * sizeof(C));
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
-  C* In = reinterpret_cast<C*>(smem_raw);                   // [ZST][N][LB]: the box layout
+  extern __shared__ __align__(1024) unsigned char zt_smem_raw[];  // TMA boxes want a 128-byte aligned base
+  C* In = reinterpret_cast<C*>(zt_smem_raw);                // [ZST][N][LB]: the box layout
   C* S = In + (size_t)ZST * N * LB;                          // the transposes, N * LB
   uint64_t* bar = reinterpret_cast<uint64_t*>(S + (size_t)N * LB);  // [ZST]
   const int total = ninst * NG, tid = threadIdx.x;

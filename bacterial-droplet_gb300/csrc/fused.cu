@@ -596,7 +596,6 @@ __global__ void __launch_bounds__(NT, 2) k_fused_rhs(const InstDev<float>* __res
 constexpr int NTC = TX * TY;            // 512 threads
 constexpr int SH = TY + 2;              // staged rows y0 - 1 .. y0 + TY
 constexpr int SW = TX + 8;              // fused_div row, floats x0 - 4 .. x0 + TX + 3
-constexpr int SPL = SW * SH;            // floats per staged plane of one field
 constexpr int CW = TX + 4;              // fused_correct row, float2 x0 - 2 .. x0 + TX + 1
 constexpr int CPL = CW * SH;            // float2 per staged plane
 constexpr int DR = 4;                   // ring slots of fused_correct
