@@ -45,8 +45,27 @@ __device__ __forceinline__ C tw(const C* t, int k) {
 
 constexpr int first_radix(int L) { return L % 4 == 0 ? 4 : (L % 2 == 0 ? 2 : (L % 3 == 0 ? 3 : 5)); }
 
+// exp(-2 pi i k / NF) from the __constant__ copy of the size-NF table (defined per size by
+// fftreg_impl.cuh): with a compile-time k it is a constant-bank operand, not a load.
+template <class C, int NF>
+__device__ C ctw(int k);
+
+// twiddle k of the DFT's table: the __constant__ copy when the line length NF is known (NF > 0),
+// else the table in global memory
+template <class C, bool INV, int NF>
+__device__ __forceinline__ C twx(const C* t, int k) {
+  if constexpr (NF > 0) {
+    C w = ctw<C, NF>(k);
+    if (INV) w.y = -w.y;
+    return w;
+  } else {
+    return tw<C, INV>(t, k);
+  }
+}
+
 // In-place DFT of v[0..L) (natural order in and out). `step` = N / L, so that w_L^m = tab[m*step].
-template <class C, int L, bool INV>
+// NF: the table's length when it has a __constant__ copy (0: read `tab`).
+template <class C, int L, bool INV, int NF = 0>
 struct Dft {
   static __device__ __forceinline__ void run(C* v, const C* tab, int step) {
     constexpr int R = first_radix(L);
@@ -71,7 +90,7 @@ struct Dft {
       for (int q = 0; q < L; ++q) {
         C acc = v[0];
 #pragma unroll
-        for (int r = 1; r < L; ++r) acc = cadd(acc, cmul(v[r], tw<C, INV>(tab, ((q * r) % L) * step)));
+        for (int r = 1; r < L; ++r) acc = cadd(acc, cmul(v[r], twx<C, INV, NF>(tab, ((q * r) % L) * step)));
         o[q] = acc;
       }
 #pragma unroll
@@ -83,14 +102,14 @@ struct Dft {
       for (int r = 0; r < R; ++r) {
 #pragma unroll
         for (int m = 0; m < M; ++m) u[r][m] = v[r + R * m];
-        Dft<C, M, INV>::run(u[r], tab, step * R);
+        Dft<C, M, INV, NF>::run(u[r], tab, step * R);
       }
 #pragma unroll
       for (int k0 = 0; k0 < M; ++k0) {
         C t[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) t[r] = (r > 0 && k0 > 0) ? cmul(u[r][k0], tw<C, INV>(tab, r * k0 * step)) : u[r][k0];
-        Dft<C, R, INV>::run(t, tab, step * M);
+        for (int r = 0; r < R; ++r) t[r] = (r > 0 && k0 > 0) ? cmul(u[r][k0], twx<C, INV, NF>(tab, r * k0 * step)) : u[r][k0];
+        Dft<C, R, INV, NF>::run(t, tab, step * M);
 #pragma unroll
         for (int k1 = 0; k1 < R; ++k1) v[k0 + M * k1] = t[k1];
       }

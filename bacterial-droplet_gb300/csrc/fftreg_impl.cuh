@@ -14,6 +14,51 @@
 namespace ttsh {
 namespace fftreg {
 
+// The sizes with a register kernel: N = N1*N2 with N2 a power of two dividing N1 and N2 as
+// large as that allows up to sqrt(N). Others use the shared-memory Stockham kernels.
+#define TTSH_FFTREG_SIZES(X) \
+  X(8, 4, 2)                 \
+  X(16, 4, 4)                \
+  X(24, 12, 2)               \
+  X(32, 8, 4)                \
+  X(48, 12, 4)               \
+  X(64, 8, 8)                \
+  X(96, 24, 4)               \
+  X(128, 16, 8)              \
+  X(160, 40, 4)              \
+  X(192, 24, 8)              \
+  X(256, 16, 16)             \
+  X(512, 32, 16)
+
+// __constant__ copies of the per-size twiddle tables (exp(-2 pi i k / N), the values of the
+// FP64-built table in global memory), filled by reg_twiddles when a size is prepared.
+#define X(n, a, b)                                                                     \
+  __constant__ float2 c_twf_##n[n];                                                    \
+  __constant__ double2 c_twd_##n[n];                                                   \
+  template <>                                                                          \
+  __device__ __forceinline__ float2 ctw<float2, n>(int k) { return c_twf_##n[k]; }      \
+  template <>                                                                          \
+  __device__ __forceinline__ double2 ctw<double2, n>(int k) { return c_twd_##n[k]; }
+TTSH_FFTREG_SIZES(X)
+#undef X
+
+template <class T>
+void reg_twiddles(int N, const void* d_tw) {
+  cudaError_t e = cudaSuccess;
+  switch (N) {
+#define X(n, a, b)                                                                                           \
+  case n:                                                                                                    \
+    if constexpr (sizeof(T) == 4) e = cudaMemcpyToSymbol(c_twf_##n, d_tw, n * sizeof(float2), 0, cudaMemcpyDeviceToDevice); \
+    else e = cudaMemcpyToSymbol(c_twd_##n, d_tw, n * sizeof(double2), 0, cudaMemcpyDeviceToDevice);           \
+    break;
+    TTSH_FFTREG_SIZES(X)
+#undef X
+    default: break;
+  }
+  if (e != cudaSuccess) throw std::runtime_error(std::string("fft (register) twiddle table: ") + cudaGetErrorString(e));
+}
+
+
 // Lines per CTA: adjacent in x for the y and z passes (coalesced 128-byte rows), consecutive
 // rows for the x pass.
 template <int N>
@@ -78,7 +123,7 @@ __device__ __forceinline__ void fft_lines(const InstDev<T>& I, int g, typename C
 #pragma unroll
       for (int n1 = 0; n1 < N1; ++n1) v[n1] = W[base + (size_t)(N2 * n1 + j) * stride];
     }
-    Dft<C, N1, false>::run(v, tab, N2);
+    Dft<C, N1, false, N>::run(v, tab, N2);
 #pragma unroll
     for (int k1 = 0; k1 < N1; ++k1) S[sidx(k1, j)] = (k1 > 0 && j > 0) ? cmul(v[k1], tw<C, false>(tab, j * k1)) : v[k1];
     __syncthreads();
@@ -89,12 +134,12 @@ __device__ __forceinline__ void fft_lines(const InstDev<T>& I, int g, typename C
       C u[N2];
 #pragma unroll
       for (int n2 = 0; n2 < N2; ++n2) u[n2] = S[sidx(k1, n2)];
-      Dft<C, N2, false>::run(u, tab, N1);
+      Dft<C, N2, false, N>::run(u, tab, N1);
       if constexpr (PASS == 2) {
         // spectrum element z = k1 + N1*k2 of the line (x = xl, y = yl): multiply, go back
 #pragma unroll
         for (int k2 = 0; k2 < N2; ++k2) u[k2] = poisson_mul(u[k2], I, xl, yl, k1 + N1 * k2);
-        Dft<C, N2, true>::run(u, tab, N1);
+        Dft<C, N2, true, N>::run(u, tab, N1);
 #pragma unroll
         for (int n2 = 0; n2 < N2; ++n2) S[sidx(k1, n2)] = (n2 > 0 && k1 > 0) ? cmul(u[n2], tw<C, true>(tab, n2 * k1)) : u[n2];
       } else {
@@ -107,7 +152,7 @@ __device__ __forceinline__ void fft_lines(const InstDev<T>& I, int g, typename C
       C x[N1];
 #pragma unroll
       for (int k1 = 0; k1 < N1; ++k1) x[k1] = S[sidx(k1, j)];
-      Dft<C, N1, true>::run(x, tab, N2);
+      Dft<C, N1, true, N>::run(x, tab, N2);
 #pragma unroll
       for (int n1 = 0; n1 < N1; ++n1) W[base + (size_t)(N2 * n1 + j) * stride] = x[n1];
     }
@@ -119,7 +164,7 @@ __device__ __forceinline__ void fft_lines(const InstDev<T>& I, int g, typename C
       C u[N2];
 #pragma unroll
       for (int k2 = 0; k2 < N2; ++k2) u[k2] = W[base + (size_t)(k1 + N1 * k2) * stride];
-      Dft<C, N2, true>::run(u, tab, N1);
+      Dft<C, N2, true, N>::run(u, tab, N1);
 #pragma unroll
       for (int n2 = 0; n2 < N2; ++n2) S[sidx(k1, n2)] = (n2 > 0 && k1 > 0) ? cmul(u[n2], tw<C, true>(tab, n2 * k1)) : u[n2];
     }
@@ -127,7 +172,7 @@ __device__ __forceinline__ void fft_lines(const InstDev<T>& I, int g, typename C
     C x[N1];
 #pragma unroll
     for (int k1 = 0; k1 < N1; ++k1) x[k1] = S[sidx(k1, j)];
-    Dft<C, N1, true>::run(x, tab, N2);
+    Dft<C, N1, true, N>::run(x, tab, N2);
 #pragma unroll
     for (int n1 = 0; n1 < N1; ++n1) {
       C v = x[n1];
@@ -415,22 +460,6 @@ void launch_size(const Group<T>& g, int pass, cudaStream_t st) {
     default: launch_pass<T, N1, N2, 4>(g, st); break;
   }
 }
-
-// The sizes with a register kernel: N = N1*N2 with N2 a power of two dividing N1 and N2 as
-// large as that allows up to sqrt(N). Others use the shared-memory Stockham kernels.
-#define TTSH_FFTREG_SIZES(X) \
-  X(8, 4, 2)                 \
-  X(16, 4, 4)                \
-  X(24, 12, 2)               \
-  X(32, 8, 4)                \
-  X(48, 12, 4)               \
-  X(64, 8, 8)                \
-  X(96, 24, 4)               \
-  X(128, 16, 8)              \
-  X(160, 40, 4)              \
-  X(192, 24, 8)              \
-  X(256, 16, 16)             \
-  X(512, 32, 16)
 
 template <class T>
 bool reg_supported(int N) {
