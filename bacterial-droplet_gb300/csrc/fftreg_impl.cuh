@@ -75,6 +75,20 @@ struct NoOp {
   __device__ __forceinline__ void operator()() const {}
 };
 
+// The four-step twiddle w_N^k of a line group: for y and z lines a warp holds two values of the
+// thread's column index, so the index takes two values per warp and the __constant__ table serves
+// it; for x lines it takes sixteen, and the table in global memory serves it.
+template <class C, bool INV, int N, int AXIS>
+__device__ __forceinline__ C tw4(const C* tab, int k) {
+  if constexpr (AXIS != 0) {
+    C w = ctw<C, N>(k);
+    if (INV) w.y = -w.y;
+    return w;
+  } else {
+    return tw<C, INV>(tab, k);
+  }
+}
+
 // PASS: 0 forward x, 1 forward y, 2 forward z + Poisson multiplier + inverse z, 3 inverse y,
 // 4 inverse x scaled by 1/N^3. One call transforms line group g of the pass (LB lines) with the
 // CTA's threads; S is the CTA's shared memory. SIN (z pass only): the group's input is already in
@@ -125,7 +139,7 @@ __device__ __forceinline__ void fft_lines(const InstDev<T>& I, int g, typename C
     }
     Dft<C, N1, false, N>::run(v, tab, N2);
 #pragma unroll
-    for (int k1 = 0; k1 < N1; ++k1) S[sidx(k1, j)] = (k1 > 0 && j > 0) ? cmul(v[k1], tw<C, false>(tab, j * k1)) : v[k1];
+    for (int k1 = 0; k1 < N1; ++k1) S[sidx(k1, j)] = (k1 > 0 && j > 0) ? cmul(v[k1], tw4<C, false, N, axis>(tab, j * k1)) : v[k1];
     __syncthreads();
     after();
 #pragma unroll
@@ -141,7 +155,7 @@ __device__ __forceinline__ void fft_lines(const InstDev<T>& I, int g, typename C
         for (int k2 = 0; k2 < N2; ++k2) u[k2] = poisson_mul(u[k2], I, xl, yl, k1 + N1 * k2);
         Dft<C, N2, true, N>::run(u, tab, N1);
 #pragma unroll
-        for (int n2 = 0; n2 < N2; ++n2) S[sidx(k1, n2)] = (n2 > 0 && k1 > 0) ? cmul(u[n2], tw<C, true>(tab, n2 * k1)) : u[n2];
+        for (int n2 = 0; n2 < N2; ++n2) S[sidx(k1, n2)] = (n2 > 0 && k1 > 0) ? cmul(u[n2], tw4<C, true, N, axis>(tab, n2 * k1)) : u[n2];
       } else {
 #pragma unroll
         for (int k2 = 0; k2 < N2; ++k2) W[base + (size_t)(k1 + N1 * k2) * stride] = u[k2];
@@ -166,7 +180,7 @@ __device__ __forceinline__ void fft_lines(const InstDev<T>& I, int g, typename C
       for (int k2 = 0; k2 < N2; ++k2) u[k2] = W[base + (size_t)(k1 + N1 * k2) * stride];
       Dft<C, N2, true, N>::run(u, tab, N1);
 #pragma unroll
-      for (int n2 = 0; n2 < N2; ++n2) S[sidx(k1, n2)] = (n2 > 0 && k1 > 0) ? cmul(u[n2], tw<C, true>(tab, n2 * k1)) : u[n2];
+      for (int n2 = 0; n2 < N2; ++n2) S[sidx(k1, n2)] = (n2 > 0 && k1 > 0) ? cmul(u[n2], tw4<C, true, N, axis>(tab, n2 * k1)) : u[n2];
     }
     __syncthreads();
     C x[N1];
