@@ -354,10 +354,11 @@ void build_engine(ttsh_sim* s, Engine<T>& E) {
     G.n = (int)E.members[g].size();
     G.N = s->inst[E.members[g][0]].N;
     G.d_err = s->d_err;
-    // FP32: the z pass with its input staged by the tensor memory accelerator where the size has
-    // it (TTSH_ZTMA=0: the z pass that loads its input directly)
+    // FP32, on request (TTSH_ZTMA=1): the z pass with its input staged by the tensor memory
+    // accelerator where the size has it; by default the z pass loads its input directly (faster
+    // since its twiddles come from constant memory)
     const char* zt = std::getenv("TTSH_ZTMA");
-    if (std::is_same<T, float>::value && !(zt && std::string(zt) == "0")) {
+    if (std::is_same<T, float>::value && zt && std::string(zt) == "1") {
       std::vector<const void*> W;
       for (int i : E.members[g]) W.push_back(E.h[i].W);
       void* maps = nullptr;

@@ -187,13 +187,13 @@ def test_plane_fft_matches_separate_passes_fp32(N, monkeypatch):
 @pytest.mark.parametrize("fft", [None, "separate"])
 def test_staged_z_pass_matches_direct_loads(fft, monkeypatch):
     """FP32, 256^3: the z pass whose input the tensor memory accelerator stages in shared memory
-    gives the same bits as the z pass that loads its input directly (TTSH_ZTMA=0)."""
+    (TTSH_ZTMA=1) gives the same bits as the z pass that loads its input directly (the default)."""
     N = 256
     st = random_state(N, seed=N + 9)
     if fft:
         monkeypatch.setenv("TTSH_FFT", fft)
     runs = {}
-    for zt in ("0", None):
+    for zt in ("1", None):
         if zt is None:
             monkeypatch.delenv("TTSH_ZTMA", raising=False)
         else:
@@ -202,7 +202,7 @@ def test_staged_z_pass_matches_direct_loads(fft, monkeypatch):
     monkeypatch.delenv("TTSH_ZTMA", raising=False)
     monkeypatch.delenv("TTSH_FFT", raising=False)
     for k in FIELDS:
-        assert np.array_equal(runs["0"][k], runs[None][k]), k
+        assert np.array_equal(runs["1"][k], runs[None][k]), k
 
 
 def test_reduce_all_matches_single_reduce():
