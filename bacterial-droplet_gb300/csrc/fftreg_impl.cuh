@@ -75,12 +75,14 @@ struct NoOp {
   __device__ __forceinline__ void operator()() const {}
 };
 
-// The four-step twiddle w_N^k of a line group: for y and z lines a warp holds two values of the
-// thread's column index, so the index takes two values per warp and the __constant__ table serves
-// it; for x lines it takes sixteen, and the table in global memory serves it.
-template <class C, bool INV, int N, int AXIS>
+// The four-step twiddle w_N^k of a line group from the __constant__ table (CONST) or the table in
+// global memory. A warp's loads of the constant table are served one distinct address at a time:
+// for y and z lines the index takes two values per warp; for x lines it takes N2 (the thread's
+// column index), and the constant table is faster only up to N2 = 8 (measured: x+y and y+x per
+// plane -8 % at 128^3, N2 = 8; +25 % at 256^3, N2 = 16).
+template <class C, bool INV, int N, bool CONST>
 __device__ __forceinline__ C tw4(const C* tab, int k) {
-  if constexpr (AXIS != 0) {
+  if constexpr (CONST) {
     C w = ctw<C, N>(k);
     if (INV) w.y = -w.y;
     return w;
@@ -102,6 +104,7 @@ __device__ __forceinline__ void fft_lines(const InstDev<T>& I, int g, typename C
   constexpr int LB = lines_per_cta<N>();
   constexpr int OW = N1 / N2;  // k1 rows owned by each thread in the second step
   constexpr int axis = (PASS == 0 || PASS == 4) ? 0 : ((PASS == 1 || PASS == 3) ? 1 : 2);
+  constexpr bool TW4C = axis != 0 || N2 <= 8;  // four-step twiddles from the constant table
   static_assert(!SIN || axis == 2, "shared-memory input: z pass only");
   C* __restrict__ W = I.W;
   const C* tab = I.tw;
@@ -139,7 +142,7 @@ __device__ __forceinline__ void fft_lines(const InstDev<T>& I, int g, typename C
     }
     Dft<C, N1, false, N>::run(v, tab, N2);
 #pragma unroll
-    for (int k1 = 0; k1 < N1; ++k1) S[sidx(k1, j)] = (k1 > 0 && j > 0) ? cmul(v[k1], tw4<C, false, N, axis>(tab, j * k1)) : v[k1];
+    for (int k1 = 0; k1 < N1; ++k1) S[sidx(k1, j)] = (k1 > 0 && j > 0) ? cmul(v[k1], tw4<C, false, N, TW4C>(tab, j * k1)) : v[k1];
     __syncthreads();
     after();
 #pragma unroll
@@ -155,7 +158,7 @@ __device__ __forceinline__ void fft_lines(const InstDev<T>& I, int g, typename C
         for (int k2 = 0; k2 < N2; ++k2) u[k2] = poisson_mul(u[k2], I, xl, yl, k1 + N1 * k2);
         Dft<C, N2, true, N>::run(u, tab, N1);
 #pragma unroll
-        for (int n2 = 0; n2 < N2; ++n2) S[sidx(k1, n2)] = (n2 > 0 && k1 > 0) ? cmul(u[n2], tw4<C, true, N, axis>(tab, n2 * k1)) : u[n2];
+        for (int n2 = 0; n2 < N2; ++n2) S[sidx(k1, n2)] = (n2 > 0 && k1 > 0) ? cmul(u[n2], tw4<C, true, N, TW4C>(tab, n2 * k1)) : u[n2];
       } else {
 #pragma unroll
         for (int k2 = 0; k2 < N2; ++k2) W[base + (size_t)(k1 + N1 * k2) * stride] = u[k2];
@@ -180,7 +183,7 @@ __device__ __forceinline__ void fft_lines(const InstDev<T>& I, int g, typename C
       for (int k2 = 0; k2 < N2; ++k2) u[k2] = W[base + (size_t)(k1 + N1 * k2) * stride];
       Dft<C, N2, true, N>::run(u, tab, N1);
 #pragma unroll
-      for (int n2 = 0; n2 < N2; ++n2) S[sidx(k1, n2)] = (n2 > 0 && k1 > 0) ? cmul(u[n2], tw4<C, true, N, axis>(tab, n2 * k1)) : u[n2];
+      for (int n2 = 0; n2 < N2; ++n2) S[sidx(k1, n2)] = (n2 > 0 && k1 > 0) ? cmul(u[n2], tw4<C, true, N, TW4C>(tab, n2 * k1)) : u[n2];
     }
     __syncthreads();
     C x[N1];
