@@ -320,10 +320,11 @@ constexpr size_t zt_smem() {
 }
 template <int N>
 constexpr int zt_min_blocks() { return 2 * zt_smem<N>() <= 227 * 1024 ? 2 : 1; }
-// The sizes with the staged z pass: CTAs of 256 threads, two per SM (N = 256). Elsewhere the
-// directly loading kernel is faster and is kept, per step (ms, CUDA events): 64 x 128^3 0.573
-// against 0.644 staged (128-thread CTAs: a quarter of the direct kernel's resident warps); 512^3
-// 0.84 against 0.98 (240 registers a thread, one CTA per SM). At 2 x 256^3 they are level.
+// The sizes with the staged z pass (on request, TTSH_ZTMA=1): CTAs of 256 threads, two per SM
+// (N = 256). The directly loading kernel is faster and is the default, per step (ms, CUDA
+// events): 64 x 128^3 0.573 against 0.644 staged (128-thread CTAs: a quarter of the direct
+// kernel's resident warps); 512^3 0.84 against 0.98 (240 registers a thread, one CTA per SM);
+// 2 x 256^3 0.128 against 0.152 once the twiddles come from the constant table.
 template <int N1, int N2>
 constexpr bool zt_has() {
   return lines_per_cta<N1 * N2>() == 16 && lines_per_cta<N1 * N2>() * N2 == 256 && N1 * N2 <= 256 &&

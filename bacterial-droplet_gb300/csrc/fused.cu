@@ -9,7 +9,8 @@
 //                 the reference's stale halo for neighbours across the periodic boundary)
 //   fused_correct u*, P*, W -> u, P   (getVNew, :505-511)
 //
-// All three march along z through a tile of TX x TY columns (a "2.5D" sweep): each z-plane of
+// All three march along z through a tile of columns (a "2.5D" sweep; fused_rhs 32 x 8, fused_div
+// 32 x 32, fused_correct 32 x 16), on a chunked or a persistent schedule: each z-plane of
 // every field the stencils need is staged once in a shared-memory ring of planes, and each
 // thread evaluates the 27-point derivatives / 15-point Laplacians of a 1 x R strip of sites
 // from its 3 x (R+2) x 3 neighbourhood, so warps read shared memory with unit stride. The
