@@ -36,6 +36,7 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "schedule.h"
 
 namespace ttsh {
 
@@ -532,13 +533,9 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
 
 // The two schedules of the three fused kernels. zc > 0: CTA (bx, by, bz) sweeps tile (bx, by)
 // (TW x TH columns) of droplet bz / nchunk over the zc planes of chunk bz % nchunk. zc == 0: a
-// persistent grid of G CTAs (as many as fit on the device at once) over the items (droplet, slab
-// of S planes, tile row, tile column): in rounds, CTA b sweeps items b, b + G, b + 2G, ... while
-// every CTA has a whole one (so the CTAs running at the same time hold neighbouring tiles of one
-// slab and meet each other's halo planes in L2, as a chunked grid does); the items left over
-// are then split into G equal contiguous runs of planes, so that no SM waits out a last partial
-// wave. seg(inst, x0, y0, z0, z1) sweeps one segment. Each kernel is built for both (PERSIST),
-// so that the chunked form carries no loop state.
+// persistent grid (as many CTAs as fit on the device at once) splits the group's sites as
+// SweepSplit (schedule.h) says. seg(inst, x0, y0, z0, z1) sweeps one segment. Each kernel is
+// built for both (PERSIST), so that the chunked form carries no loop state.
 template <int TW, int TH, bool PERSIST, class F>
 __device__ __forceinline__ void sweep_schedule(int N, int nchunk, int zc, int ninst, F&& seg) {
   if constexpr (!PERSIST) {
@@ -546,34 +543,11 @@ __device__ __forceinline__ void sweep_schedule(int N, int nchunk, int zc, int ni
     seg((int)(blockIdx.z / nchunk), (int)blockIdx.x * TW, (int)blockIdx.y * TH, z0, min(z0 + zc, N));
     return;
   }
-  const int TXN = N / TW, TPI = TXN * (N / TH);  // tile columns per row, per droplet
-  int S = N;                                     // slab height: a divisor of N, at most 128 where N allows
-  while (S > 128 && S % 2 == 0) S /= 2;
-  const int NS = N / S;
-  const int items = ninst * NS * TPI, G = gridDim.x;
-  const int full = items / G;
-  const long long rest = (long long)(items - full * G) * S;  // planes of the items left over
-  long long w = (long long)blockIdx.x * rest / G;
-  const long long w1 = (long long)(blockIdx.x + 1) * rest / G;
-  int k = 0;
-  for (;;) {  // one call site of seg: the rounds, then this CTA's run of the rest
-    int item, za, zb;
-    if (k < full) {
-      item = k++ * G + (int)blockIdx.x;
-      za = 0;
-      zb = S;
-    } else if (w < w1) {
-      const int q = (int)(w / S);
-      za = (int)(w - (long long)q * S);
-      zb = (int)min((long long)S, za + (w1 - w));
-      item = full * G + q;
-      w += zb - za;
-    } else {
-      break;
-    }
-    const int inst = item / (NS * TPI), r = item - inst * NS * TPI;
-    const int sl = r / TPI, t = r - sl * TPI;
-    seg(inst, (t % TXN) * TW, (t / TXN) * TH, sl * S + za, sl * S + zb);
+  const int TXN = N / TW;  // tile columns per row
+  SweepSplit split(N, TXN * (N / TH), ninst, (int)gridDim.x, (int)blockIdx.x);
+  int inst, t, z0, z1;
+  while (split.next(inst, t, z0, z1)) {  // one call site of seg
+    seg(inst, (t % TXN) * TW, (t / TXN) * TH, z0, z1);
     __syncthreads();  // the next segment refills the rings the last one read
   }
 }
