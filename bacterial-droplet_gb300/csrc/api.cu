@@ -292,7 +292,7 @@ void build_engine(ttsh_sim* s, Engine<T>& E) {
     t.Ct = reinterpret_cast<T*>(d + off); CK(cudaMemcpy(d + off, Ct.data(), N * sizeof(T), cudaMemcpyHostToDevice));
     tab[N] = t;
     fft_prepare<T>(N);
-    if (fftreg_has<T>(N)) fftreg_twiddles<T>(N, t.tw);
+    if (fftreg_has<T>(N)) fftreg_twiddles<T>(N);
   }
   // per-instance arenas
   for (int i = 0; i < n; ++i) {

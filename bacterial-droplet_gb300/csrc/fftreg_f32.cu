@@ -20,8 +20,8 @@ void fftreg_prepare<float>(int N) {
   fftreg::reg_prepare<float>(N);
 }
 template <>
-void fftreg_twiddles<float>(int N, const void* d_tw) {
-  fftreg::reg_twiddles<float>(N, d_tw);
+void fftreg_twiddles<float>(int N) {
+  fftreg::reg_twiddles<float>(N);
 }
 
 int fftreg_zt_setup(int N, const std::vector<const void*>& W, void** d_maps) {

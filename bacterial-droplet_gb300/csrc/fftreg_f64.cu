@@ -20,8 +20,8 @@ void fftreg_prepare<double>(int N) {
   fftreg::reg_prepare<double>(N);
 }
 template <>
-void fftreg_twiddles<double>(int N, const void* d_tw) {
-  fftreg::reg_twiddles<double>(N, d_tw);
+void fftreg_twiddles<double>(int N) {
+  fftreg::reg_twiddles<double>(N);
 }
 
 }  // namespace ttsh

@@ -4,8 +4,10 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cmath>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "common.cuh"
 #include "fftreg.cuh"
@@ -31,7 +33,8 @@ namespace fftreg {
   X(512, 32, 16)
 
 // __constant__ copies of the per-size twiddle tables (exp(-2 pi i k / N), the values of the
-// FP64-built table in global memory), filled by reg_twiddles when a size is prepared.
+// FP64-built table in global memory), filled by reg_twiddles when a size is prepared (every
+// register FFT kernel of the size reads them).
 #define X(n, a, b)                                                                     \
   __constant__ float2 c_twf_##n[n];                                                    \
   __constant__ double2 c_twd_##n[n];                                                   \
@@ -43,13 +46,22 @@ TTSH_FFTREG_SIZES(X)
 #undef X
 
 template <class T>
-void reg_twiddles(int N, const void* d_tw) {
+void reg_twiddles(int N) {
+  typedef typename CxT<T>::type C;
+  // exp(-2 pi i k / N) formed in FP64 and rounded to T, as the table in global memory is
+  const double kPi = 3.1415926535897932384626433832795;
+  std::vector<C> tw(N);
+  for (int k = 0; k < N; ++k) {
+    const double a = -2.0 * kPi * (double)k / (double)N;
+    tw[k].x = (T)std::cos(a);
+    tw[k].y = (T)std::sin(a);
+  }
   cudaError_t e = cudaSuccess;
   switch (N) {
-#define X(n, a, b)                                                                                           \
-  case n:                                                                                                    \
-    if constexpr (sizeof(T) == 4) e = cudaMemcpyToSymbol(c_twf_##n, d_tw, n * sizeof(float2), 0, cudaMemcpyDeviceToDevice); \
-    else e = cudaMemcpyToSymbol(c_twd_##n, d_tw, n * sizeof(double2), 0, cudaMemcpyDeviceToDevice);           \
+#define X(n, a, b)                                                                          \
+  case n:                                                                                   \
+    if constexpr (sizeof(T) == 4) e = cudaMemcpyToSymbol(c_twf_##n, tw.data(), n * sizeof(C)); \
+    else e = cudaMemcpyToSymbol(c_twd_##n, tw.data(), n * sizeof(C));                       \
     break;
     TTSH_FFTREG_SIZES(X)
 #undef X

@@ -49,8 +49,9 @@ template <class T> int fft_lines(const Group<T>& g);
 // Register-resident FFT passes (fftreg_*.cu): false when the size has none (Stockham is used).
 template <class T> bool fftreg_launch(const Group<T>& g, int pass, cudaStream_t st);
 template <class T> void fftreg_prepare(int N);
-// Copies the size-N twiddle table d_tw (device memory) into the register FFT's __constant__ copy.
-template <class T> void fftreg_twiddles(int N, const void* d_tw);
+// Fills the register FFT's __constant__ twiddle table of size N on the current device (its
+// kernels read it; call once per device and size before they run; allocates nothing).
+template <class T> void fftreg_twiddles(int N);
 template <class T> bool fftreg_has(int N);
 // Forward x + y (dir 0) or inverse y + x (dir 1) of every z-plane, one CTA per plane (fft_kind 2):
 // false when the group does not use it.

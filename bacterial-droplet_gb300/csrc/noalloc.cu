@@ -113,6 +113,7 @@ extern "C" int ttsh_step_noalloc(const ttsh_input* in, const ttsh_ext* ext, int 
       std::lock_guard<std::mutex> lk(g_mu);
       if (!g_prepared[dev][N]) {
         fft_prepare<double>(N);
+        if (fftreg_has<double>(N)) fftreg_twiddles<double>(N);  // the register FFT's constant table
         g_prepared[dev][N] = true;
       }
     }

@@ -84,3 +84,52 @@ def test_step_noalloc_rejects_sizes_beyond_its_working_memory():
     rc = ttsh.lib().ttsh_step_noalloc(ctypes.byref(inp), ctypes.byref(ext), 1, p, p, p, p, p, p, p, None)
     assert rc == ttsh.E_UNSUPPORTED
     assert b"outside" in ttsh.lib().ttsh_last_error()
+
+
+_FRESH = r"""
+import ctypes, sys
+import numpy as np
+import torch
+sys.path.insert(0, sys.argv[1])
+sys.path.insert(0, sys.argv[2])
+import ttsh
+from conftest import random_state
+N = 24
+st = random_state(N, seed=78)
+inp = ttsh.default_input(Nx=N, Ny=N, Nz=N)
+ext = ttsh.default_ext(precision=64, zeta=0.02)
+dev = torch.device("cuda", 0)
+d = {k: torch.tensor(st[k], device=dev, dtype=torch.float64) for k in ("phi", "P", "u", "us", "ps")}
+d["pv"] = torch.zeros((N, N, N), device=dev, dtype=torch.float64)
+d["pp"] = torch.zeros((N, N, N), device=dev, dtype=torch.float64)
+lib = ttsh.lib()
+# the no-allocation step first: nothing else in this process has prepared size N
+rc = lib.ttsh_step_noalloc(ctypes.byref(inp), ctypes.byref(ext), 2, d["phi"].data_ptr(), d["P"].data_ptr(),
+                           d["u"].data_ptr(), d["us"].data_ptr(), d["ps"].data_ptr(), d["pv"].data_ptr(),
+                           d["pp"].data_ptr(), torch.cuda.current_stream(dev).cuda_stream)
+assert rc == ttsh.OK, lib.ttsh_last_error().decode()
+torch.cuda.synchronize(dev)
+got = {k: d[k].cpu().numpy() for k in ("phi", "P", "u", "pv", "pp")}
+with ttsh.Sim(inp, ext) as s:
+    s.set_state(0, st["phi"], st["P"], st["u"], st["us"], st["ps"])
+    s.step(2)
+    want = s.get_state(0)
+for k in got:
+    nb = np.linalg.norm(want[k])
+    err = float(np.linalg.norm(got[k] - want[k]) / (nb if nb > 0 else 1.0))
+    assert err <= 1e-11, (k, err)
+print("ok")
+"""
+
+
+def test_step_noalloc_first_in_a_fresh_process():
+    """The no-allocation step prepares everything its kernels read (the FFT's constant twiddle
+    table included) by itself: run first in a fresh process, before any ttsh_create of the size,
+    it still matches the regular entry points."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, "-c", _FRESH, os.path.join(root, "bacterial-droplet_gb300"),
+                          os.path.join(root, "tests")], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0 and out.stdout.strip().endswith("ok"), out.stdout[-2000:] + out.stderr[-2000:]
