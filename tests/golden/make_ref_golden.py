@@ -110,4 +110,6 @@ def main(outdir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "gpurun_out", "golden"))
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: python tests/golden/make_ref_golden.py OUTDIR")
+    main(sys.argv[1])
