@@ -90,6 +90,57 @@ _D = ctypes.POINTER(ctypes.c_double)
 _VP = ctypes.c_void_p
 
 
+def _signatures():
+    """ctypes argument and result types of every C-ABI entry point the binding uses."""
+    return {
+        "ttsh_read_input": ([ctypes.c_char_p, ctypes.POINTER(Input)], ctypes.c_int),
+        "ttsh_default_input": ([ctypes.POINTER(Input)], None),
+        "ttsh_default_ext": ([ctypes.POINTER(Ext)], None),
+        "ttsh_create": ([ctypes.POINTER(Input), ctypes.POINTER(Ext), ctypes.c_int, ctypes.POINTER(_VP)],
+                        ctypes.c_int),
+        "ttsh_batch_create": ([ctypes.POINTER(Input), ctypes.POINTER(Ext), ctypes.c_int, ctypes.c_int,
+                               ctypes.POINTER(_VP)], ctypes.c_int),
+        "ttsh_set_stream": ([_VP, _VP], ctypes.c_int),
+        "ttsh_set_state": ([_VP, ctypes.c_int, _D, _D, _D, _D, _D], ctypes.c_int),
+        "ttsh_init_droplet": ([ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                               ctypes.c_double, _D, _D], ctypes.c_int),
+        "ttsh_step": ([_VP, ctypes.c_int], ctypes.c_int),
+        "ttsh_sync": ([_VP], ctypes.c_int),
+        "ttsh_get_state": ([_VP, ctypes.c_int, _D, _D, _D, _D, _D], ctypes.c_int),
+        "ttsh_get_provisional": ([_VP, ctypes.c_int, _D, _D], ctypes.c_int),
+        "ttsh_reduce": ([_VP, ctypes.c_int, ctypes.POINTER(Stats)], ctypes.c_int),
+        "ttsh_write_conf": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),
+        "ttsh_reduce_all": ([_VP, ctypes.c_int, ctypes.POINTER(Stats)], ctypes.c_int),
+        "ttsh_format_conf": ([ctypes.c_int, ctypes.c_int, _D, _D, _D, ctypes.c_char_p], ctypes.c_int),
+        "ttsh_destroy": ([_VP], None),
+        "ttsh_strerror": ([ctypes.c_int], ctypes.c_char_p),
+        "ttsh_last_error": ([], ctypes.c_char_p),
+        "ttsh_num_instances": ([_VP], ctypes.c_int),
+        "ttsh_instance_n": ([_VP, ctypes.c_int], ctypes.c_int),
+        "ttsh_time": ([_VP], ctypes.c_double),
+        "ttsh_profile_kernels": ([_VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), _D,
+                                  ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+        "ttsh_launches_per_step": ([_VP], ctypes.c_int),
+        "ttsh_struct_size": ([ctypes.c_int], ctypes.c_int),
+        "ttsh_save_checkpoint": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),
+        "ttsh_init_reference": ([ctypes.POINTER(Input), ctypes.c_uint, ctypes.c_char_p, _D, _D, _D, _D, _D],
+                                ctypes.c_int),
+        "ttsh_run_dirs": ([ctypes.POINTER(ctypes.c_char_p), ctypes.c_int, ctypes.POINTER(Ext), ctypes.c_uint64,
+                           ctypes.c_int], ctypes.c_int),
+        "ttsh_snapshot_slice": ([_VP, ctypes.c_int, _D, ctypes.POINTER(ctypes.c_int), _D], ctypes.c_int),
+        "ttsh_load_checkpoint": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),
+        "ttsh_partials_size": ([_VP], ctypes.c_size_t),
+        "ttsh_reduce_all_async": ([_VP, ctypes.c_int, _D], ctypes.c_int),
+        "ttsh_stats_from_partials": ([_VP, _D, ctypes.POINTER(Stats)], ctypes.c_int),
+        "ttsh_num_groups": ([_VP], ctypes.c_int),
+        "ttsh_get_tuning": ([_VP, ctypes.c_int, ctypes.POINTER(Tuning)], ctypes.c_int),
+        "ttsh_set_tuning": ([_VP, ctypes.c_int, ctypes.POINTER(Tuning)], ctypes.c_int),
+        "ttsh_autotune": ([_VP, ctypes.c_char_p], ctypes.c_int),
+        "ttsh_step_noalloc": ([ctypes.POINTER(Input), ctypes.POINTER(Ext), ctypes.c_int] + [_VP] * 7 + [_VP],
+                              ctypes.c_int),
+    }
+
+
 def lib():
     """Load libttsh.so (building it first if it is absent)."""
     global _lib
@@ -98,53 +149,7 @@ def lib():
             from . import build as _b
             _b.build()
         L = ctypes.CDLL(LIB_PATH)
-        sig = {
-            "ttsh_read_input": ([ctypes.c_char_p, ctypes.POINTER(Input)], ctypes.c_int),
-            "ttsh_default_input": ([ctypes.POINTER(Input)], None),
-            "ttsh_default_ext": ([ctypes.POINTER(Ext)], None),
-            "ttsh_create": ([ctypes.POINTER(Input), ctypes.POINTER(Ext), ctypes.c_int, ctypes.POINTER(_VP)],
-                            ctypes.c_int),
-            "ttsh_batch_create": ([ctypes.POINTER(Input), ctypes.POINTER(Ext), ctypes.c_int, ctypes.c_int,
-                                   ctypes.POINTER(_VP)], ctypes.c_int),
-            "ttsh_set_stream": ([_VP, _VP], ctypes.c_int),
-            "ttsh_set_state": ([_VP, ctypes.c_int, _D, _D, _D, _D, _D], ctypes.c_int),
-            "ttsh_init_droplet": ([ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
-                                   ctypes.c_double, _D, _D], ctypes.c_int),
-            "ttsh_step": ([_VP, ctypes.c_int], ctypes.c_int),
-            "ttsh_sync": ([_VP], ctypes.c_int),
-            "ttsh_get_state": ([_VP, ctypes.c_int, _D, _D, _D, _D, _D], ctypes.c_int),
-            "ttsh_get_provisional": ([_VP, ctypes.c_int, _D, _D], ctypes.c_int),
-            "ttsh_reduce": ([_VP, ctypes.c_int, ctypes.POINTER(Stats)], ctypes.c_int),
-            "ttsh_write_conf": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),
-            "ttsh_reduce_all": ([_VP, ctypes.c_int, ctypes.POINTER(Stats)], ctypes.c_int),
-            "ttsh_format_conf": ([ctypes.c_int, ctypes.c_int, _D, _D, _D, ctypes.c_char_p], ctypes.c_int),
-            "ttsh_destroy": ([_VP], None),
-            "ttsh_strerror": ([ctypes.c_int], ctypes.c_char_p),
-            "ttsh_last_error": ([], ctypes.c_char_p),
-            "ttsh_num_instances": ([_VP], ctypes.c_int),
-            "ttsh_instance_n": ([_VP, ctypes.c_int], ctypes.c_int),
-            "ttsh_time": ([_VP], ctypes.c_double),
-            "ttsh_profile_kernels": ([_VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p), _D,
-                                      ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
-            "ttsh_launches_per_step": ([_VP], ctypes.c_int),
-            "ttsh_struct_size": ([ctypes.c_int], ctypes.c_int),
-            "ttsh_save_checkpoint": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),
-            "ttsh_init_reference": ([ctypes.POINTER(Input), ctypes.c_uint, ctypes.c_char_p, _D, _D, _D, _D, _D],
-                                    ctypes.c_int),
-            "ttsh_run_dirs": ([ctypes.POINTER(ctypes.c_char_p), ctypes.c_int, ctypes.POINTER(Ext), ctypes.c_uint64,
-                               ctypes.c_int], ctypes.c_int),
-            "ttsh_snapshot_slice": ([_VP, ctypes.c_int, _D, ctypes.POINTER(ctypes.c_int), _D], ctypes.c_int),
-            "ttsh_load_checkpoint": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),
-            "ttsh_partials_size": ([_VP], ctypes.c_size_t),
-            "ttsh_reduce_all_async": ([_VP, ctypes.c_int, _D], ctypes.c_int),
-            "ttsh_stats_from_partials": ([_VP, _D, ctypes.POINTER(Stats)], ctypes.c_int),
-            "ttsh_num_groups": ([_VP], ctypes.c_int),
-            "ttsh_get_tuning": ([_VP, ctypes.c_int, ctypes.POINTER(Tuning)], ctypes.c_int),
-            "ttsh_set_tuning": ([_VP, ctypes.c_int, ctypes.POINTER(Tuning)], ctypes.c_int),
-            "ttsh_autotune": ([_VP, ctypes.c_char_p], ctypes.c_int),
-            "ttsh_step_noalloc": ([ctypes.POINTER(Input), ctypes.POINTER(Ext), ctypes.c_int] + [_VP] * 7 + [_VP],
-                                  ctypes.c_int),
-        }
+        sig = _signatures()
         for name, (args, res) in sig.items():
             f = getattr(L, name)
             f.argtypes = args

@@ -191,3 +191,27 @@ def test_struct_layouts_match_the_library():
     for k, cls in enumerate((ttsh.Input, ttsh.Ext, ttsh.Stats, ttsh.Tuning)):
         assert L.ttsh_struct_size(k) == ctypes.sizeof(cls), cls.__name__
     assert L.ttsh_struct_size(4) == -1
+
+
+def test_binding_signatures_match_header():
+    """Every entry point the ctypes binding declares exists in include/ttsh.h with the same number
+    of parameters and a result of the same kind (int, double, size_t, string, void)."""
+    import ctypes
+    import re
+    import ttsh
+    text = open(os.path.join(ROOT, "include", "ttsh.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    text = "\n".join(l for l in text.split("\n") if not l.lstrip().startswith("#"))  # preprocessor lines
+    decls = {}
+    for m in re.finditer(r"([A-Za-z_][\w\s\*]*?)\b(ttsh_\w+)\s*\(([^;{)]*)\)\s*;", text):
+        ret, name, params = " ".join(m.group(1).split()), m.group(2), m.group(3).strip()
+        n = 0 if params in ("", "void") else params.count(",") + 1
+        decls[name] = (ret, n)
+    kind = {ctypes.c_int: "int", ctypes.c_double: "double", ctypes.c_size_t: "size_t", ctypes.c_char_p: "const char*",
+            None: "void"}
+    for name, (args, res) in ttsh._signatures().items():
+        assert name in decls, name
+        ret, n = decls[name]
+        assert n == len(args), (name, n, len(args))
+        assert kind[res] == ret.replace("const char *", "const char*"), (name, ret, kind[res])
