@@ -179,11 +179,10 @@ def init_states(ttsh, drops, pinned: bool):
 def cpu_baseline_sample():
     """The FP64 oracle (C++/OpenMP restatement) on one 256^3 droplet for 2 steps, host cores."""
     import oracle
-    import ttsh
     oracle.build()
     n = oracle.set_threads(os.cpu_count() or 1)
     N, steps = 256, 2
-    phi, P = ttsh.init_droplet(N, 64.0, 2.0, 1)
+    phi, P = oracle.init_droplet(N, 64.0, 2.0, 1)
     s = oracle.new_state(N)
     s["phi"][:] = phi
     s["px"][:], s["py"][:], s["pz"][:] = P
@@ -206,10 +205,12 @@ def run_reference(args):
     except Exception as e:  # report and fall back
         out["note"] = "reference program not built: %s" % str(e)[:200]
     if binary:
+        # nothing of libttsh is loaded here: the input file is written in Python and the initial
+        # fields come from the oracle's restatement of the droplet construction (same bits)
         import make_ref_golden as G
-        import ttsh
+        import oracle
         N = 256
-        phi, P = ttsh.init_droplet(N, 64.0, 2.0, 1)
+        phi, P = oracle.init_droplet(N, 64.0, 2.0, 1)
         st = {k: np.zeros((N, N, N)) for k in G.FIELDS}
         st["phi"] = phi
         st["px"], st["py"], st["pz"] = P
@@ -252,6 +253,7 @@ def main():
     ap.add_argument("--form", type=int, default=0, choices=[0, 1, 2], help="0 auto, 1 plain, 2 fused")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 one-droplet reference point")
     ap.add_argument("--no-tune", action="store_true", help="keep the default kernel configuration")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -366,6 +368,29 @@ def main():
                        "pinned host FP64 arrays; wall clock" % args.steps, "split": split,
                "clocks": eclocks}
 
+    # the other side of the metric: the plain FP64 form, one 256^3 droplet per launch (R = 64,
+    # xi = 2, seed 1, zeta = 0.02), on the same GPU in the same run, CUDA events around its steps
+    fp64 = None
+    if not args.no_fp64 and args.precision == 32:
+        k64 = max(3, min(args.steps, 10))
+        with make_sim(ttsh, [(256, 64.0, 2.0, 1, 0.02)], 64, k2_mode=args.k2, form=1) as s64:
+            s64.set_stream(stream.cuda_stream)
+            phi, P, u, _ = init_states(ttsh, [(256, 64.0, 2.0, 1, 0.02)], pinned=False)[0]
+            s64.set_state(0, phi, P, u)
+            s64.step(3)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            s64.step(k64)
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms64 = replicas.max_over_ranks(a.elapsed_time(b), device="cuda")
+        v64 = 256 ** 3 * world * k64 / (ms64 / 1e3) / 1e6
+        fp64 = {"value": v64, "unit": UNIT, "ms_per_step": ms64 / k64, "steps": k64, "warmup": 3,
+                "workload": "1 x 256^3 (R=64, xi=2, seed 1, zeta=0.02), FP64 plain form (one droplet per launch, "
+                            "the reference's arithmetic order), same GPU and run",
+                "ratio_fp32_batched_over_fp64_plain": value / v64}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample()
@@ -402,6 +427,8 @@ def main():
         }
         if e2e:
             line["e2e"] = e2e
+        if fp64:
+            line["fp64_plain"] = fp64
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line))

@@ -34,7 +34,10 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF_SRC = "/root/reference/bacterial_droplet_12-16/TTSH3D.cu"
+# The reference checkout this recipe reads (development container only; never on the GPU machine).
+REF_ROOT = os.environ.get("TTSH_REFERENCE_ROOT", "/root/reference")
+REF_DIR = os.path.join(REF_ROOT, "bacterial_droplet_12-16")
+REF_SRC = os.path.join(REF_DIR, "TTSH3D.cu")
 GEN = os.path.join(OUT, "TTSH3D_ref.cu")
 BIN = os.path.join(OUT, "ttsh_ref.out")
 

@@ -67,6 +67,8 @@ def lib():
         _lib.orc_mass.restype = ctypes.c_double
         _lib.orc_max_div.argtypes = [d, d, d, ctypes.c_int, ctypes.c_double]
         _lib.orc_max_div.restype = ctypes.c_double
+        _lib.orc_init_droplet.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_uint64, ctypes.c_double, d, d]
         _lib.orc_set_threads.argtypes = [ctypes.c_int]
         _lib.orc_set_threads.restype = ctypes.c_int
     return _lib
@@ -126,6 +128,15 @@ def project(xs, ys, zs, h: float, dt: float, k2_mode: int = 0) -> np.ndarray:
     out = np.empty_like(xs)
     lib().orc_project(_ptr(xs), _ptr(ys), _ptr(zs), xs.shape[0], h, dt, k2_mode, _ptr(out))
     return out
+
+
+def init_droplet(N: int, R: float, xi: float, seed: int, h: float = 1.0, angular_noise: float = 0.0):
+    """The benchmark droplet's initial (phi, P), restated from libttsh's ttsh_init_droplet (same bits)."""
+    phi = np.zeros((N, N, N))
+    P = np.zeros((3, N, N, N))
+    if lib().orc_init_droplet(N, h, R, xi, seed, angular_noise, _ptr(phi), _ptr(P)) != 0:
+        raise ValueError("orc_init_droplet: bad arguments")
+    return phi, P
 
 
 def mass(phi: np.ndarray, h: float = 1.0) -> float:

@@ -28,6 +28,7 @@
 //
 // Arithmetic is FP64 everywhere. Compile with -ffp-contract=off so that x86
 // and aarch64 builds give identical bits (no reductions depend on thread count).
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -436,6 +437,75 @@ void orc_project(const double* xs, const double* ys, const double* zs, int N, do
   const double* X[3] = {xs, ys, zs};
   const double* O[3] = {nullptr, nullptr, nullptr};
   project(p, w, X, O, out);
+}
+
+// The droplet initial condition of the benchmark workloads (a build-defined extension of the
+// reference, whose InitConf has no seed, radius or width; TTSH3D.cu:801-824): phi =
+// (1 - tanh((r - R)/xi))/2 about the box centre; inside (phi > 0.5) a unit direction uniform on
+// the sphere from a counter-based generator (splitmix64 of seed and site), optionally tilted by
+// Gaussian angular noise; three Jacobi passes (mean of the site and its 6 face neighbours,
+// periodic); P zeroed again where phi <= 0.5. The same draws and operation order as libttsh's
+// ttsh_init_droplet, so both give the same bits with the same compiler flags; the timed
+// reference arm builds its input with this one and never loads libttsh.
+static inline uint64_t orc_splitmix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+static inline double orc_uni(uint64_t seed, uint64_t idx, uint64_t k) {
+  return (double)(orc_splitmix64(orc_splitmix64(seed) ^ (idx * 8 + k)) >> 11) * (1.0 / 9007199254740992.0);
+}
+
+int orc_init_droplet(int N, double h, double R, double xi, uint64_t seed, double angular_noise, double* phi,
+                     double* P) {
+  if (N < 4 || !(h > 0) || !(xi > 0) || !phi || !P) return 1;
+  const size_t n = (size_t)N * N * N;
+  const double c = N / 2.0, twopi = 6.283185307179586476925286766559;
+  std::vector<double> Q(3 * n, 0.0), T(3 * n);
+  for (int z = 0; z < N; ++z)
+    for (int y = 0; y < N; ++y)
+      for (int x = 0; x < N; ++x) {
+        const size_t i = ((size_t)z * N + y) * N + x;
+        const double dx = x - c, dy = y - c, dz = z - c;
+        phi[i] = 0.5 * (1.0 - std::tanh((h * std::sqrt(dx * dx + dy * dy + dz * dz) - R) / xi));
+        if (!(phi[i] > 0.5)) continue;
+        const double cz = 1.0 - 2.0 * orc_uni(seed, i, 0), az = twopi * orc_uni(seed, i, 1);
+        const double s = std::sqrt(std::max(0.0, 1.0 - cz * cz));
+        double v[3] = {s * std::cos(az), s * std::sin(az), cz};
+        if (angular_noise > 0) {
+          double g[3], w[3], nn = 0;
+          for (int k = 0; k < 3; ++k) {
+            const double u1 = 1.0 - orc_uni(seed, i, 2 + k), u2 = orc_uni(seed, i, 5 + (k % 3));
+            g[k] = std::sqrt(-2.0 * std::log(u1)) * std::cos(twopi * u2);
+          }
+          const double gp = g[0] * v[0] + g[1] * v[1] + g[2] * v[2];
+          for (int k = 0; k < 3; ++k) {
+            w[k] = v[k] + angular_noise * (g[k] - gp * v[k]);
+            nn += w[k] * w[k];
+          }
+          nn = std::sqrt(nn);
+          for (int k = 0; k < 3; ++k) v[k] = w[k] / nn;
+        }
+        for (int k = 0; k < 3; ++k) Q[k * n + i] = v[k];
+      }
+  for (int pass = 0; pass < 3; ++pass) {
+    for (int k = 0; k < 3; ++k) {
+      const double* a = &Q[k * n];
+      double* b = &T[k * n];
+      for (int z = 0; z < N; ++z)
+        for (int y = 0; y < N; ++y)
+          for (int x = 0; x < N; ++x) {
+            auto at = [&](int X, int Y, int Z) { return a[((size_t)wrap(Z, N) * N + wrap(Y, N)) * N + wrap(X, N)]; };
+            b[((size_t)z * N + y) * N + x] = (at(x, y, z) + at(x - 1, y, z) + at(x + 1, y, z) + at(x, y - 1, z) +
+                                              at(x, y + 1, z) + at(x, y, z - 1) + at(x, y, z + 1)) / 7.0;
+          }
+    }
+    Q.swap(T);
+  }
+  for (size_t i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) P[k * n + i] = phi[i] > 0.5 ? Q[k * n + i] : 0.0;
+  return 0;
 }
 
 // FP64 mass sum(phi) h^3, serial (order fixed).

@@ -11,7 +11,10 @@ import subprocess
 import sys
 import tempfile
 
-REF = "/root/reference/bacterial_droplet_12-16/run_cuda.pl"
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))), "oracle"))
+from make_ref import REF_DIR  # noqa: E402
+
+REF = os.path.join(REF_DIR, "run_cuda.pl")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "input_default.dat")
 
 

@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN, ROOT
+from make_ref import REF_DIR  # oracle/ is on the path (conftest)
 
 
 def test_library_exports_every_declared_symbol():
@@ -166,7 +167,7 @@ def test_golden_fixture_script_is_committed():
     assert os.path.exists(os.path.join(ROOT, "tests", "golden", "make_input_dat.py"))
 
 
-OP_PY = "/root/reference/bacterial_droplet_12-16/op.py"
+OP_PY = os.path.join(REF_DIR, "op.py")
 
 
 @pytest.mark.skipif(not os.path.exists(OP_PY), reason="reference sources not present")
@@ -215,3 +216,24 @@ def test_binding_signatures_match_header():
         ret, n = decls[name]
         assert n == len(args), (name, n, len(args))
         assert kind[res] == ret.replace("const char *", "const char*"), (name, ret, kind[res])
+
+
+def test_oracle_init_droplet_is_the_library_one():
+    """The oracle's restatement of the benchmark droplet (used by the timed reference arm, which must
+    not load libttsh) gives exactly libttsh's ttsh_init_droplet, with and without angular noise."""
+    import oracle
+    import ttsh
+    for (N, R, xi, seed, noise) in ((20, 5.0, 2.0, 3, 0.0), (24, 7.2, 3.0, 7, 0.01), (16, 4.0, 2.0, 1, 0.0)):
+        a = ttsh.init_droplet(N, R, xi, seed, angular_noise=noise)
+        b = oracle.init_droplet(N, R, xi, seed, angular_noise=noise)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), (N, seed, noise)
+
+
+def test_reference_input_text_is_the_writer_output(tmp_path):
+    """The pure-Python input.dat of the reference arm is byte for byte what ttsh.write_input prints."""
+    import make_ref_golden as G
+    import ttsh
+    for (N, Ts, dte, expo) in ((256, 0.0495, 1e9, 0), (12, 0.009, 0.004, 1), (64, 1000.0, 10.0, 1)):
+        p = tmp_path / ("in_%d.dat" % N)
+        ttsh.write_input(str(p), ttsh.default_input(Nx=N, Ny=N, Nz=N, Ts=Ts, dte=dte, ExpoData=expo))
+        assert G.reference_input_text(N, Ts, dte, expo) == p.read_text(), N
