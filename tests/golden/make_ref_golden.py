@@ -8,7 +8,6 @@ Writes to OUTDIR:
   ref_N12.npz          init and final fields (15 each, FP64, [z,y,x]) of a 5-step run at 12^3
   ref_N12_input.dat    the input.dat used (reference defaults except N, Ts, dte, ExpoData)
   ref_N12_conf_<te>.dat  the reference's own snapshot files (ExpoConf text layout)
-  ref_N12_log.txt      the program's stdout
 The fixtures are committed under tests/golden/ and checked by the CPU tests (oracle vs
 reference, snapshot writer byte-for-byte vs the reference's ExpoConf).
 """
@@ -119,8 +118,7 @@ def main(outdir):
     for f in sorted(os.listdir(os.path.join(work, "data_1"))):
         if f.startswith("conf_"):
             shutil.copy(os.path.join(work, "data_1", f), os.path.join(outdir, "ref_N12_" + f))
-    with open(os.path.join(outdir, "ref_N12_log.txt"), "w") as fh:
-        fh.write(log)
+    print(log.strip().splitlines()[-1] if log.strip() else "")
     shutil.rmtree(work, ignore_errors=True)
     print("golden written to", outdir)
 
