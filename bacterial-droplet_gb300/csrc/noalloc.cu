@@ -17,9 +17,15 @@
 //     at zero (each step writes every scratch word it later reads). Calls whose GPU work
 //     overlaps — on two streams, or from two host threads — race on the array: serialise them.
 //   * The first call on a device looks up the array's device address (cudaGetSymbolAddress,
-//     with that device current) and sets the FFT kernels' shared-memory limits; make that first
-//     call before any stream capture is started on the calling thread.
-// The kernels are the plain-form kernels of plain.cu and fft.cu, unchanged.
+//     with that device current); the first call for a size on a device sets the FFT kernels'
+//     shared-memory limits and fills the register FFT's constant twiddle table, then waits for
+//     the device to finish (that table is written through the legacy stream, which a caller's
+//     non-blocking stream does not wait for). Make those first calls before any stream capture
+//     is started on the calling thread.
+//   * Every later call only enqueues work on the caller's stream: the tables and the droplet
+//     descriptor travel as the parameter of a small set-up kernel (copied at launch), not through
+//     host memory that a copy would have to wait for or outlive.
+// The step kernels are the plain-form kernels of plain.cu and fft.cu, unchanged.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -27,7 +33,6 @@
 #include <mutex>
 #include <stdexcept>
 #include <string>
-#include <vector>
 
 #include "../../include/ttsh.h"
 #include "common.cuh"
@@ -60,6 +65,22 @@ void* g_addr[256] = {nullptr};
 bool g_prepared[256][kMaxN + 1] = {{false}};
 
 int fail(int code, const std::string& msg) { return ttsh::set_error(code, "ttsh_step_noalloc: " + msg); }
+
+// What one call writes into the tail of the working array before its steps: the droplet
+// descriptor, the twiddles exp(-2 pi i k / N) and the wavenumber tables (k, k^2, sin(k h)/h,
+// (2 + cos(k h))/3), passed by value as a kernel parameter (about 2 KB, within the 4 KB limit).
+struct Setup {
+  ttsh::InstDev<double> inst;
+  double2 tw[kMaxN];
+  double tab[4 * kMaxN];
+};
+static_assert(sizeof(Setup) <= 4000, "set-up parameter within the kernel parameter limit");
+
+__global__ void k_noalloc_setup(const Setup s, ttsh::InstDev<double>* d_inst, double2* d_tw, double* d_tab) {
+  for (int i = threadIdx.x; i < kMaxN; i += blockDim.x) d_tw[i] = s.tw[i];
+  for (int i = threadIdx.x; i < 4 * kMaxN; i += blockDim.x) d_tab[i] = s.tab[i];
+  if (threadIdx.x == 0) *d_inst = s.inst;
+}
 
 // Once per device (that device current): the device address of g_noalloc_scratch.
 int noalloc_scratch_address(int dev, unsigned char** out) {
@@ -114,13 +135,17 @@ extern "C" int ttsh_step_noalloc(const ttsh_input* in, const ttsh_ext* ext, int 
       if (!g_prepared[dev][N]) {
         fft_prepare<double>(N);
         if (fftreg_has<double>(N)) fftreg_twiddles<double>(N);  // the register FFT's constant table
+        // the table copy runs on the legacy stream: let it land before kernels on any stream read it
+        const cudaError_t es = cudaDeviceSynchronize();
+        if (es != cudaSuccess) throw std::runtime_error(std::string("first-call set-up: ") + cudaGetErrorString(es));
         g_prepared[dev][N] = true;
       }
     }
     const size_t n = (size_t)N * N * N;
     // carve the scratch: fields first (each sized for N), then tables, then the descriptor
     double* f = reinterpret_cast<double*>(base);
-    InstDev<double> I{};
+    Setup su{};
+    InstDev<double>& I = su.inst;
     size_t off = 0;
     auto take = [&](size_t count) { double* p = f + off; off += count; return p; };
     I.mu0 = take(n);
@@ -139,18 +164,16 @@ extern "C" int ttsh_step_noalloc(const ttsh_input* in, const ttsh_ext* ext, int 
     InstDev<double>* d_inst = reinterpret_cast<InstDev<double>*>(tail + 32768);
 
     // the same tables and constants as ttsh_create builds (api.cu)
-    std::vector<double2> tw(N);
-    std::vector<double> tab(4 * kMaxN, 0.0);
     const double h = in->h;
     for (int k = 0; k < N; ++k) {
       const double a = -2.0 * kPi * (double)k / (double)N;
-      tw[k] = make_double2(std::cos(a), std::sin(a));
+      su.tw[k] = make_double2(std::cos(a), std::sin(a));
       double kk = 2 * kPi * k / (N * h + 0.0);
       if (k >= N / 2) kk = 2 * kPi * (k - N) / (N * h + 0.0);
-      tab[k] = kk;
-      tab[kMaxN + k] = kk * kk;
-      tab[2 * kMaxN + k] = std::sin(kk * h) / h;
-      tab[3 * kMaxN + k] = (2.0 + std::cos(kk * h)) / 3.0;
+      su.tab[k] = kk;
+      su.tab[kMaxN + k] = kk * kk;
+      su.tab[2 * kMaxN + k] = std::sin(kk * h) / h;
+      su.tab[3 * kMaxN + k] = (2.0 + std::cos(kk * h)) / 3.0;
     }
     I.N = N;
     I.stale = (ext->quirks & TTSH_QUIRK_STALE_HALO) ? 1 : 0;
@@ -182,10 +205,9 @@ extern "C" int ttsh_step_noalloc(const ttsh_input* in, const ttsh_ext* ext, int 
     cudaError_t e_ = (call);                                                        \
     if (e_ != cudaSuccess) throw std::runtime_error(std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
-    // pageable sources: these copies return once the data has been staged
-    NA_CK(cudaMemcpyAsync(d_tw, tw.data(), N * sizeof(double2), cudaMemcpyHostToDevice, st));
-    NA_CK(cudaMemcpyAsync(d_kval, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-    NA_CK(cudaMemcpyAsync(d_inst, &I, sizeof(I), cudaMemcpyHostToDevice, st));
+    // descriptor and tables into the working array, in stream order, by value (no host copy)
+    k_noalloc_setup<<<1, 128, 0, st>>>(su, d_inst, d_tw, d_kval);
+    NA_CK(cudaGetLastError());
     Group<double> g{d_inst, 1, N};
     for (int t = 0; t < nsteps; ++t) {
       launch_stage1<double>(g, 0, st);

@@ -268,12 +268,15 @@ int ttsh_launches_per_step(const ttsh_sim* s);
  *   ustar, Pstar (3*N^3): on entry the previous step's u*, P* (zeros at the start; they feed the
  *     stale-halo divergence), on return this call's last u*, P*.
  *   p_v, p_p (N^3): outputs, the last projection's pressures (untouched when nsteps == 0).
- *   stream: cudaStream_t as void* (NULL = legacy default stream); the call is asynchronous.
+ *   stream: cudaStream_t as void* (NULL = legacy default stream). The call enqueues its work on
+ *     that stream and returns without waiting for it or for earlier work (the tables and the
+ *     droplet descriptor travel as a kernel parameter, not through a host-to-device copy).
  * Rejects N > TTSH_NOALLOC_MAX_N, non-cubic grids and precision != 64 with TTSH_E_UNSUPPORTED.
  * All calls share the working array and leave its contents behind (nothing in it must start
  * at zero); calls whose GPU work overlaps race on it and must be serialised by the caller.
- * The first call on a device looks up the array's device address and sets kernel attributes;
- * make that first call before starting any stream capture on the calling thread. */
+ * The first call on a device looks up the array's device address; the first call for a size on
+ * a device also sets kernel attributes, fills a constant table and waits for the device to
+ * finish. Make those first calls before starting any stream capture on the calling thread. */
 int ttsh_step_noalloc(const ttsh_input* in, const ttsh_ext* ext, int nsteps, double* phi, double* P, double* u,
                       double* ustar, double* Pstar, double* p_v, double* p_p, void* stream);
 

@@ -2,11 +2,14 @@
 
 Such callers (their GPU memory is owned by another allocator or capped per process, or they
 cannot afford cudaFree's device-wide wait) hand in their own device arrays; the step's working
-memory is a fixed array inside libttsh. This test calls the entry point through the C ABI twice
-in a row on device buffers the test owns and checks each result against the regular entry points
-(ttsh_create / ttsh_set_state / ttsh_step / ttsh_get_state) run on the same inputs. Tolerance:
-1e-11 relative L2 per field, the FP64 tolerance of the other GPU tests (the two paths run the same
-kernels, so the results are expected to agree exactly). Kept in its own file, collected last.
+memory is a fixed array inside libttsh. These tests call the entry point through the C ABI twice
+in a row on device buffers the test owns and check each result against the regular entry points
+(ttsh_create / ttsh_set_state / ttsh_step / ttsh_get_state) run on the same inputs: the two paths
+run the same kernels in the same order, so the results must be identical bit for bit (the FP64
+tolerance of the other GPU tests, 1e-11 relative L2, would hide a changed kernel). Sizes from the
+smallest (8) to the largest the working array holds (32, which fills it), with and without the
+stale-halo quirk, on torch's current stream and on a non-blocking stream. Kept in its own file,
+collected last.
 """
 import ctypes
 
@@ -17,60 +20,51 @@ from conftest import random_state
 
 pytestmark = pytest.mark.gpu
 
-TOL = 1e-11
+
+def _regular(inp, ext, st, counts):
+    import ttsh
+    out = []
+    with ttsh.Sim(inp, ext) as s:
+        s.set_state(0, st["phi"], st["P"], st["u"], st["us"], st["ps"])
+        for k in counts:
+            s.step(k)
+            w = s.get_state(0)
+            w["us"], w["ps"] = s.get_provisional(0)
+            out.append(w)
+    return out
 
 
-def _rel(a, b):
-    nb = np.linalg.norm(b)
-    return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
-
-
-def test_step_noalloc_matches_step_two_calls():
+@pytest.mark.parametrize("N,quirks,nonblocking", [(8, 1, False), (24, 1, False), (32, 1, False), (32, 0, False),
+                                                  (24, 0, True), (32, 1, True)])
+def test_step_noalloc_matches_step_two_calls(N, quirks, nonblocking):
     import torch
     import ttsh
 
-    N = 24
-    st = random_state(N, seed=77)
+    st = random_state(N, seed=77 + N)
     inp = ttsh.default_input(Nx=N, Ny=N, Nz=N)
-    ext = ttsh.default_ext(precision=64, zeta=0.02)
-
-    # regular entry points: 3 steps, then 2 more
-    with ttsh.Sim(inp, ext) as s:
-        s.set_state(0, st["phi"], st["P"], st["u"], st["us"], st["ps"])
-        s.step(3)
-        want1 = s.get_state(0)
-        want1["us"], want1["ps"] = s.get_provisional(0)
-        s.step(2)
-        want2 = s.get_state(0)
-        want2["us"], want2["ps"] = s.get_provisional(0)
+    ext = ttsh.default_ext(precision=64, zeta=0.02, quirks=quirks)
+    want = _regular(inp, ext, st, (3, 2))  # 3 steps, then 2 more
 
     dev = torch.device("cuda", 0)
-    d = {
-        "phi": torch.tensor(st["phi"], device=dev, dtype=torch.float64),
-        "P": torch.tensor(st["P"], device=dev, dtype=torch.float64),
-        "u": torch.tensor(st["u"], device=dev, dtype=torch.float64),
-        "us": torch.tensor(st["us"], device=dev, dtype=torch.float64),
-        "ps": torch.tensor(st["ps"], device=dev, dtype=torch.float64),
-        "pv": torch.zeros((N, N, N), device=dev, dtype=torch.float64),
-        "pp": torch.zeros((N, N, N), device=dev, dtype=torch.float64),
-    }
-    stream = torch.cuda.current_stream(dev).cuda_stream
+    d = {k: torch.tensor(st[k], device=dev, dtype=torch.float64) for k in ("phi", "P", "u", "us", "ps")}
+    d["pv"] = torch.zeros((N, N, N), device=dev, dtype=torch.float64)
+    d["pp"] = torch.zeros((N, N, N), device=dev, dtype=torch.float64)
+    torch.cuda.synchronize(dev)  # the buffers are ready before a stream that does not wait for others
+    stream = torch.cuda.Stream(dev) if nonblocking else torch.cuda.current_stream(dev)
     lib = ttsh.lib()
 
     def call(nsteps):
         rc = lib.ttsh_step_noalloc(ctypes.byref(inp), ctypes.byref(ext), nsteps, d["phi"].data_ptr(),
                                    d["P"].data_ptr(), d["u"].data_ptr(), d["us"].data_ptr(), d["ps"].data_ptr(),
-                                   d["pv"].data_ptr(), d["pp"].data_ptr(), stream)
+                                   d["pv"].data_ptr(), d["pp"].data_ptr(), stream.cuda_stream)
         assert rc == ttsh.OK, lib.ttsh_last_error().decode()
-        torch.cuda.synchronize(dev)
+        stream.synchronize()
 
-    for nsteps, want in ((3, want1), (2, want2)):
+    for nsteps, w in zip((3, 2), want):
         call(nsteps)
-        got = {"phi": d["phi"].cpu().numpy(), "P": d["P"].cpu().numpy(), "u": d["u"].cpu().numpy(),
-               "pv": d["pv"].cpu().numpy(), "pp": d["pp"].cpu().numpy(), "us": d["us"].cpu().numpy(),
-               "ps": d["ps"].cpu().numpy()}
-        errs = {k: _rel(got[k], want[k]) for k in got}
-        assert max(errs.values()) <= TOL, (nsteps, errs)
+        for k in ("phi", "P", "u", "pv", "pp", "us", "ps"):
+            got = d[k].cpu().numpy()
+            assert np.array_equal(got, w[k]), (nsteps, k, float(np.abs(got - w[k]).max()))
 
 
 def test_step_noalloc_rejects_sizes_beyond_its_working_memory():
@@ -115,9 +109,7 @@ with ttsh.Sim(inp, ext) as s:
     s.step(2)
     want = s.get_state(0)
 for k in got:
-    nb = np.linalg.norm(want[k])
-    err = float(np.linalg.norm(got[k] - want[k]) / (nb if nb > 0 else 1.0))
-    assert err <= 1e-11, (k, err)
+    assert np.array_equal(got[k], want[k]), (k, float(np.abs(got[k] - want[k]).max()))
 print("ok")
 """
 
