@@ -229,6 +229,7 @@ Phys<T> make_phys(const ttsh_input& in, const ttsh_ext& ext) {
   p.cl12 = (T)(1.0 / (12 * h * h));
   p.cl23 = (T)(2.0 / (3 * h * h));
   p.cl143 = (T)(14.0 / (3 * h * h));
+  p.clz = (T)(1.0 / (h * h));
   const double n3 = (double)in.Nx * in.Nx * in.Nx;
   p.invN3 = (T)(1.0 / n3);
   return p;
@@ -365,6 +366,9 @@ void build_engine(ttsh_sim* s, Engine<T>& E) {
       G.zt_grid = fftreg_zt_setup(G.N, W, &maps);
       if (maps) s->tables.push_back(maps);
       G.d_tmz = maps;
+      // failure test only: every CTA skips its first copy and its wait for it runs out
+      const char* drop = std::getenv("TTSH_TEST_DROP_STAGED_COPY");
+      G.zt_drop = (drop && std::string(drop) == "1") ? 1 : 0;
     }
     std::vector<InstDev<T>> arr;
     for (int i : E.members[g]) arr.push_back(E.h[i]);

@@ -309,13 +309,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
       : "memory");
   return done != 0;
 }
-// Waits for phase `parity` of the barrier for at most 2^31 SM clocks (about a second); false when
-// that limit ran out.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* b, unsigned parity) {
+// Waits for phase `parity` of the barrier for at most `limit` SM clocks (2^31, about a second, on
+// the step); false when that limit ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* b, unsigned parity, long long limit = 1ll << 31) {
   if (mbar_try_wait(b, parity)) return true;
   const long long t0 = clock64();
   while (!mbar_try_wait(b, parity))
-    if (clock64() - t0 > (1ll << 31)) return false;
+    if (clock64() - t0 > limit) return false;
   return true;
 }
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
@@ -346,7 +346,7 @@ constexpr bool zt_has() {
 template <int N1, int N2>
 __global__ void __launch_bounds__(lines_per_cta<N1 * N2>() * N2, zt_min_blocks<N1 * N2>())
     k_fftz_tma(const InstDev<float>* __restrict__ insts, const CUtensorMap* __restrict__ maps, int ninst,
-               int* __restrict__ err) {
+               int* __restrict__ err, int drop_first) {
   typedef float2 C;
   constexpr int N = N1 * N2, LB = lines_per_cta<N>(), NGX = N / LB, NG = N * NGX;
   constexpr int NBOX = (N + 255) / 256, BZ = N / NBOX;
@@ -365,6 +365,11 @@ __global__ void __launch_bounds__(lines_per_cta<N1 * N2>() * N2, zt_min_blocks<N
     for (int b = 0; b < NBOX; ++b)
       tma_load_3d(In + ((size_t)s * N + (size_t)b * BZ) * LB, maps + inst, 2 * x, y, b * BZ, &bar[s]);
   };
+  // issued[s] (used by thread 0): the CTA-local index k of the last group whose copy went to stage
+  // s, or -1
+  int issued[ZST];
+#pragma unroll
+  for (int s = 0; s < ZST; ++s) issued[s] = -1;
   if (tid == 0) {
     for (int s = 0; s < ZST; ++s) mbar_init(&bar[s], 1);
     mbar_fence_init();
@@ -372,26 +377,36 @@ __global__ void __launch_bounds__(lines_per_cta<N1 * N2>() * N2, zt_min_blocks<N
   __syncthreads();
   if (tid == 0)
     for (int s = 0; s < ZST; ++s)
-      if (blockIdx.x + s * gridDim.x < total) issue(blockIdx.x + s * gridDim.x, s);
+      if (blockIdx.x + s * gridDim.x < total && !(drop_first && s == 0)) {
+        issue(blockIdx.x + s * gridDim.x, s);
+        issued[s] = s;
+      }
+  // the failure test shortens the wait so that the dropped copy's wait runs out quickly
+  const long long limit = drop_first ? (1ll << 20) : (1ll << 31);
   int k = 0;
   bool ok = true;
   for (int g = blockIdx.x; g < total; g += gridDim.x, ++k) {
     const int s = k % ZST;
     // every thread observes the copy complete (acquire); the CTA goes on only if all did
-    ok = __syncthreads_and(mbar_wait_bounded(&bar[s], (unsigned)(k / ZST) & 1u)) != 0;
+    ok = __syncthreads_and(mbar_wait_bounded(&bar[s], (unsigned)(k / ZST) & 1u, limit)) != 0;
     if (!ok) break;
     const int inst = g / NG, gn = g + ZST * gridDim.x;
     fft_lines<float, N1, N2, 2, true>(insts[inst], g - inst * NG, S, In + (size_t)s * N * LB, [&] {
-      if (tid == 0 && gn < total) issue(gn, s);
+      if (tid == 0 && gn < total) {
+        issue(gn, s);
+        issued[s] = k + ZST;
+      }
     });
   }
   if (!ok) {
-    // a copy did not complete in time: report it and wait (bounded) for this CTA's copies still
-    // in flight, groups k .. k + ZST - 1, before the CTA's shared memory is released
+    // a copy did not complete in time: report it, then wait for this CTA's copies still in
+    // flight (issued to a stage for group k or later) before its shared memory is released.
+    // That wait is bounded too (2^31 clocks); were it to run out, the CTA would leave with a copy
+    // still writing, and the context as a whole is to be treated as unreliable after this error.
     if (tid == 0) {
       atomicExch(err, 1);
-      for (int kk = k; kk < k + ZST; ++kk)
-        if (blockIdx.x + kk * gridDim.x < total) mbar_wait_bounded(&bar[kk % ZST], (unsigned)(kk / ZST) & 1u);
+      for (int q = 0; q < ZST; ++q)
+        if (issued[q] >= k) mbar_wait_bounded(&bar[q], (unsigned)(issued[q] / ZST) & 1u);
     }
     __syncthreads();
   }
@@ -403,7 +418,7 @@ void launch_zt(const Group<float>& g, cudaStream_t st) {
   const int total = g.n * N * (N / LB);
   const int grid = total < g.zt_grid ? total : g.zt_grid;
   k_fftz_tma<N1, N2><<<grid, LB * N2, zt_smem<N>(), st>>>(g.d_inst, reinterpret_cast<const CUtensorMap*>(g.d_tmz),
-                                                          g.n, g.d_err);
+                                                          g.n, g.d_err, g.zt_drop);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) throw std::runtime_error(std::string("fft (staged z) launch: ") + cudaGetErrorString(e));
 }

@@ -25,6 +25,8 @@ struct Group {
   // complex field (device array of n CUtensorMap) and the persistent grid (0: not used)
   void* d_tmz = nullptr;
   int zt_grid = 0;
+  int zt_drop = 0;       // failure test only (TTSH_TEST_DROP_STAGED_COPY=1): each CTA of the staged
+                         // z pass skips its first copy, so that its bounded wait runs out (short limit)
   int* d_err = nullptr;  // set to 1 by a kernel whose bounded wait for its input ran out
 };
 

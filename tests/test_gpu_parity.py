@@ -33,10 +33,10 @@ def run_gpu(st, nsteps, precision=64, k2_mode=0, quirks=1, zeta=0.0, **inp_kw):
     return out
 
 
-def run_oracle(O, st, nsteps, k2_mode=0, stale=1, zeta=0.0):
+def run_oracle(O, st, nsteps, k2_mode=0, stale=1, zeta=0.0, **consts):
     N = st["phi"].shape[0]
     s = oracle_state(st)
-    O.step(s, nsteps, N, k2_mode=k2_mode, stale_halo=stale, zeta=zeta)
+    O.step(s, nsteps, N, k2_mode=k2_mode, stale_halo=stale, zeta=zeta, **consts)
     return dict(phi=s["phi"], P=np.stack([s["px"], s["py"], s["pz"]]), u=np.stack([s["vx"], s["vy"], s["vz"]]),
                 pv=s["pv"], pp=s["pp"], us=np.stack([s["vxs"], s["vys"], s["vzs"]]),
                 ps=np.stack([s["pxs"], s["pys"], s["pzs"]]))
