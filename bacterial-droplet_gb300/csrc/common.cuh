@@ -19,6 +19,7 @@ struct Phys {
   T mu, cA, alpha, beta, eta, La2, kappa, lambda0, aPhi2, kPhi, gamma, A, zeta;
   T c2h;           // 1/(2h)
   T cl12, cl23, cl143;  // 1/(12h^2), 2/(3h^2), 14/(3h^2)
+  T clz;           // 1/h^2 (the fused form's shift-invariant Laplacian)
   T invN3;         // 1/N^3 (FP32 path); FP64 path divides by (double)N^3 as getStream mode 2
   double dt_d;     // dt in FP64 (divisor of getStream mode 0 in the FP64 path)
 };

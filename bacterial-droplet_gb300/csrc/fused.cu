@@ -117,12 +117,20 @@ __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b
 
 // Separable evaluation (FP32). With s = [1, 4, 1] and delta = [-1, 0, 1]:
 //   D_x = c2h/36 * delta_x s_y s_z,  D_y = c2h/36 * s_x delta_y s_z,  D_z = c2h/36 * s_x s_y delta_z,
-//   L = cl12 * (8 corners) + cl23 * (6 faces) - cl143 * centre  (corners = c_x c_y c_z, c = [1, 0, 1]),
+//   L = cl12 * (8 corners - 8 centre) + cl23 * (6 faces - 6 centre)  (corners = c_x c_y c_z,
+//       c = [1, 0, 1]),
 // the reference's 27-point and 15-point weights (TTSH3D.cu:3280-3343) regrouped. Each row of the
 // neighbourhood (3 planes x 3 columns) is reduced to the few sums the R sites of the strip share.
+// The Laplacian is written shift-invariant: the reference's -14/(3h^2) centre weight is split
+// between the two neighbour sums (8 cl12 + 6 cl23 = 14/(3h^2)), each of which subtracts the centre
+// before its weight is applied, so that a constant field has exactly zero Laplacian in FP32. With
+// the three weights rounded to FP32 separately, L(1) would be about 2.4e-7/h^2 instead of zero: a
+// systematic term, e.g. a spurious -kPhi 2.4e-7 phi in mu_0, whose force mu_0 D phi is a gradient
+// that the pressure absorbs as a smooth error.
 struct SepK {
   float d;  // c2h / 36
   float l12, l23, l143;
+  float lz;  // 1/h^2 = 4 l12 + l23 (the z-carried form's weight of the centre column)
 };
 // ld(z, r, c): the value at plane z (0..2 = offset -1..1), strip row r (0..R+1 = offset -1..R),
 // column c (0..2 = offset -1..1). ctr[i] receives the centre value of site i.
@@ -156,10 +164,13 @@ __device__ __forceinline__ void sep_rows(const LD& ld, const SepK& k, V* dx, V* 
     if (DY) dy[i] = vmul(kd, vsub(b[i + 2], b[i]));
     if (DZ) dz[i] = vmul(kd, vfma(four, c[i + 1], vadd(c[i], c[i + 2])));
     if (LAP) {
+      const V c = h[i + 1];
       const V corners = vadd(e[i], e[i + 2]);
       const V faces = vadd(vadd(f[i + 1], g[i + 1]), vadd(h[i], h[i + 2]));
-      lap[i] = vfma(vsplat(k.l12, V()), corners,
-                    vfma(vsplat(k.l23, V()), faces, vmul(vsplat(-k.l143, V()), h[i + 1])));
+      // corners - 8c: 8c is exact; faces - 6c with 6c rounded as the sum of the faces is, so that
+      // both differences vanish exactly for a constant field
+      lap[i] = vfma(vsplat(k.l12, V()), vfma(vsplat(-8.f, V()), c, corners),
+                    vmul(vsplat(k.l23, V()), vsub(faces, vmul(vsplat(6.f, V()), c))));
     }
     if (ctr) ctr[i] = h[i + 1];
   }
@@ -170,7 +181,7 @@ __device__ __forceinline__ void sep_rows(const LD& ld, const SepK& k, V* dx, V* 
 __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, int N, int x0, int y0, int z0, int z1,
                                             unsigned char* smr) {
   const Phys<float> p = I.ph;  // by value: read once, kept in registers
-  const SepK sk{p.c2h * (1.f / 36.f), p.cl12, p.cl23, p.cl143};
+  const SepK sk{p.c2h * (1.f / 36.f), p.cl12, p.cl23, p.cl143, p.clz};
   const size_t NN = (size_t)N * N;
   const float* __restrict__ gphi = I.phi[par];
   const float* __restrict__ gP[3] = {I.P[0], I.P[1], I.P[2]};
@@ -309,7 +320,10 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
         const int o = (by0 + k) * BP + bx;
         const float ph = C0[k].x, px = C0[k].y, py = C1[k].x, pz = C1[k].y;
         // mu_0 = aPhi 2(phi - 3phi^2 + 2phi^3) - kPhi L phi (:567), mu_b = phi P_b + La^2 L P_b (:571-573)
-        const float poly = p.aPhi2 * (ph - 3 * ph * ph + 2 * ph * ph * ph);
+        // 2 aPhi (phi - 3 phi^2 + 2 phi^3) factored as 2 aPhi phi (1 - phi)(1 - 2 phi): for phi near 0
+        // or 1 (inside and outside the droplet) the reference's expanded form cancels to a small
+        // value that FP32 would resolve only to about 1e-7
+        const float poly = p.aPhi2 * (ph * ((1.f - ph) * (1.f - 2.f * ph)));
         const float2 M0 = vfma(f2(-p.kPhi, p.La2), L0[k], f2(poly, ph * px));
         const float2 M1 = vfma(vsplat(p.La2, float2()), L1[k], vmul(vsplat(ph, float2()), C1[k]));
         sPr[PM0 * BNP + o] = M0;
@@ -414,11 +428,15 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
             for (int c = 0; c < 3; ++c) v[r][c] = F[r * BP + c];
 #pragma unroll
           for (int k = 0; k < 2; ++k) {
+            // shift-invariant in-plane sums (see SepK): an off-centre plane adds
+            // G = l12 (4 diagonals - 4 centre) + lz centre, the centre plane
+            // H = l23 (4 edges - 4 centre) - 2 lz centre; G + H + G = L, zero for a constant field
             const float2 ce = v[k + 1][1];
             const float2 dg = vadd(vadd(v[k][0], v[k][2]), vadd(v[k + 2][0], v[k + 2][2]));
             const float2 ed = vadd(vadd(v[k][1], v[k + 2][1]), vadd(v[k + 1][0], v[k + 1][2]));
-            const float2 G = vfma(vsplat(sk.l12, float2()), dg, vmul(vsplat(sk.l23, float2()), ce));
-            const float2 H = vfma(vsplat(sk.l23, float2()), ed, vmul(vsplat(-sk.l143, float2()), ce));
+            const float2 four_c = vmul(four, ce);
+            const float2 G = vfma(vsplat(sk.l12, float2()), vsub(dg, four_c), vmul(vsplat(sk.lz, float2()), ce));
+            const float2 H = vfma(vsplat(sk.l23, float2()), vsub(ed, four_c), vmul(vsplat(-2.f * sk.lz, float2()), ce));
             lm[k][q] = vadd(cv2[k * 2 + q], G);
             cv2[k * 2 + q] = vadd(cv2[4 + k * 2 + q], H);
             cv2[4 + k * 2 + q] = G;
