@@ -334,6 +334,14 @@ void build_engine(ttsh_sim* s, Engine<T>& E) {
     }
     I.W = reinterpret_cast<C*>(d + off);
   }
+  if constexpr (std::is_same<T, float>::value) {
+    // the per-droplet maxima of the packed Poisson source (two ints each), for its balancing
+    int* wm = nullptr;
+    CK(cudaMalloc(&wm, 2 * sizeof(int) * (size_t)n));
+    CK(cudaMemset(wm, 0, 2 * sizeof(int) * (size_t)n));
+    s->tables.push_back(wm);
+    for (int i = 0; i < n; ++i) E.h[i].wmax = wm + 2 * i;
+  }
   if (!s->d_err) {
     CK(cudaMalloc(&s->d_err, sizeof(int)));
     CK(cudaMemset(s->d_err, 0, sizeof(int)));
@@ -593,6 +601,7 @@ struct TrialBackup {
       for (int b = 0; b < 3; ++b) arrays.push_back({I.P[b], n * sizeof(T)});
       if (I.phic) arrays.push_back({I.phic, n * sizeof(T)});
       arrays.push_back({I.W, 2 * n * sizeof(T)});
+      if (I.wmax) arrays.push_back({I.wmax, 2 * sizeof(int)});  // the pressures' scales
     }
     size_t tot = 0;
     for (auto& a : arrays) tot += a.second;
@@ -759,13 +768,14 @@ static void h2d(T* dst, const double* src, size_t n, cudaStream_t st, double* sc
   }
 }
 template <class T>
-static void d2h(double* dst, const T* src, size_t n, cudaStream_t st, double* scratch, size_t stride = 1) {
+static void d2h(double* dst, const T* src, size_t n, cudaStream_t st, double* scratch, size_t stride = 1,
+                double scale = 1.0) {
   if constexpr (sizeof(T) == sizeof(double)) {
     if (stride == 1) CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, st));
     else CK(cudaMemcpy2DAsync(dst, sizeof(double), src, stride * sizeof(double), sizeof(double), n,
                               cudaMemcpyDeviceToHost, st));
   } else {
-    launch_to_f64(src, stride, scratch, n, st);
+    launch_to_f64(src, stride, scratch, n, scale, st);
     CK(cudaMemcpyAsync(dst, scratch, n * sizeof(double), cudaMemcpyDeviceToHost, st));
   }
 }
@@ -990,8 +1000,16 @@ int ttsh_get_state(ttsh_sim* s, int inst, double* phi, double* P, double* u, dou
         if (u) d2h<TT>(u + b * n, I.U[b], n, s->stream, scr);
       }
       const TT* w = reinterpret_cast<const TT*>(I.W);
-      if (p_v) d2h<TT>(p_v, w, n, s->stream, scr, 2);
-      if (p_p) d2h<TT>(p_p, w + 1, n, s->stream, scr, 2);
+      double sv = 1.0, sp = 1.0;  // FP32: the pressures' power-of-two scales (pow2_norm, common.cuh)
+      if (I.wmax && (p_v || p_p)) {
+        int wm[2];
+        CK(cudaMemcpyAsync(wm, I.wmax, sizeof wm, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        sv = pow2_denorm(wm[0]);
+        sp = pow2_denorm(wm[1]);
+      }
+      if (p_v) d2h<TT>(p_v, w, n, s->stream, scr, 2, sv);
+      if (p_p) d2h<TT>(p_p, w + 1, n, s->stream, scr, 2, sp);
       CK(cudaStreamSynchronize(s->stream));
     });
     return kernel_error(s);

@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 namespace ttsh {
 
@@ -40,6 +41,8 @@ struct InstDev {
   T* Ps[2][3];
   C* W;               // N^3 complex: (div u* + i div P*)/dt -> (p_v + i p_p)
   T* phic;            // fused form: compensation of the phi update (the low part lost to rounding)
+  int* wmax;          // FP32 forms: max |Re W|, max |Im W| of this step's Poisson source (float bits,
+                      // non-negative floats order as ints); null in the FP64 form
   T* mu0;             // plain-form intermediates
   T* mu[3];
   T* sig[9];          // sig[a*3+b] = phi * D_a P_b
@@ -52,6 +55,47 @@ struct InstDev {
 };
 
 __host__ __device__ inline int wrapi(int a, int N) { return a < 0 ? a + N : (a >= N ? a - N : a); }
+
+// The packed Poisson source W = D.u*/dt + i D.P*/dt of the FP32 forms is transformed as one
+// complex field. Its two parts can differ in size by orders of magnitude (the divergence of the
+// polarisation is large while P is far from solenoidal), and the rounding of every complex
+// operation is relative to the larger part: in FP32 that error would swamp the smaller part (a
+// relative error of 1e-4 in p_v when |D.P*| is 500 x |D.u*|). So the first forward pass scales
+// each part by the power of two that brings its maximum into [1, 2), and the correction (and the
+// read-back of the pressures) undoes it; powers of two scale exactly, so only the balance changes.
+// Scale for a maximum given as float bits (0: no scaling).
+__host__ __device__ inline float pow2_norm(int mbits) {
+  if (mbits <= 0) return 1.f;
+  int e = ((mbits >> 23) & 0xff) - 127;
+  e = e < -125 ? -125 : (e > 125 ? 125 : e);
+  const unsigned bits = (unsigned)(127 - e) << 23;
+  float s;
+  memcpy(&s, &bits, sizeof s);
+  return s;
+}
+// Its inverse, exact.
+__host__ __device__ inline float pow2_denorm(int mbits) {
+  if (mbits <= 0) return 1.f;
+  int e = ((mbits >> 23) & 0xff) - 127;
+  e = e < -125 ? -125 : (e > 125 ? 125 : e);
+  const unsigned bits = (unsigned)(127 + e) << 23;
+  float s;
+  memcpy(&s, &bits, sizeof s);
+  return s;
+}
+// Warp-aggregated record of the source's maxima |Re|, |Im| (float bits) into wmax[0..1]; any
+// subset of a warp's lanes may call it.
+__device__ __forceinline__ void record_wmax(int* wmax, float ax, float ay) {
+  const unsigned act = __activemask();
+  const unsigned mx = __reduce_max_sync(act, __float_as_uint(fabsf(ax)));
+  const unsigned my = __reduce_max_sync(act, __float_as_uint(fabsf(ay)));
+  unsigned lane;
+  asm("mov.u32 %0, %%laneid;" : "=r"(lane));
+  if (lane == (unsigned)(__ffs(act) - 1)) {
+    atomicMax(wmax, (int)mx);
+    atomicMax(wmax + 1, (int)my);
+  }
+}
 
 // Accessor of a scalar field around (x,y,z) with periodic wrap.
 template <class T>

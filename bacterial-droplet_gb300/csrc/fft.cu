@@ -134,13 +134,23 @@ __global__ void __launch_bounds__(FFT_THREADS) k_fft(const InstDev<T>* __restric
     if (axis == 1) { base0 = (size_t)outer * NN + x0; stride = N; }
     else { base0 = (size_t)outer * N + x0; stride = NN; lineY = outer; }
   }
-  // load
+  // load (FP32, first forward pass: both parts of the packed source brought to the same size,
+  // pow2_norm in common.cuh)
+  T su = T(1), sp = T(1);
+  if constexpr (PASS == 0 && sizeof(T) == 4) {
+    if (I.wmax) {
+      su = pow2_norm(I.wmax[0]);
+      sp = pow2_norm(I.wmax[1]);
+    }
+  }
   for (int t = threadIdx.x; t < LB * N; t += blockDim.x) {
     int l, e;
     size_t src;
     if (axis == 0) { l = t / N; e = t - l * N; src = base0 + t; }
     else { e = t / LB; l = t - e * LB; src = base0 + (size_t)e * stride + l; }
-    buf0[l * pitch + e] = W[src];
+    C v = W[src];
+    if constexpr (PASS == 0 && sizeof(T) == 4) { v.x *= su; v.y *= sp; }
+    buf0[l * pitch + e] = v;
   }
   __syncthreads();
   const bool inv = (PASS == 3 || PASS == 4);

@@ -152,6 +152,14 @@ __device__ __forceinline__ void fft_lines(const InstDev<T>& I, int g, typename C
 #pragma unroll
       for (int n1 = 0; n1 < N1; ++n1) v[n1] = W[base + (size_t)(N2 * n1 + j) * stride];
     }
+    if constexpr (PASS == 0 && sizeof(T) == 4) {
+      // FP32: both parts of the packed source brought to the same size (pow2_norm, common.cuh)
+      if (I.wmax) {
+        const T su = pow2_norm(I.wmax[0]), sp = pow2_norm(I.wmax[1]);
+#pragma unroll
+        for (int n1 = 0; n1 < N1; ++n1) { v[n1].x *= su; v[n1].y *= sp; }
+      }
+    }
     Dft<C, N1, false, N>::run(v, tab, N2);
 #pragma unroll
     for (int k1 = 0; k1 < N1; ++k1) S[sidx(k1, j)] = (k1 > 0 && j > 0) ? cmul(v[k1], tw4<C, false, N, TW4C>(tab, j * k1)) : v[k1];

@@ -575,6 +575,9 @@ __global__ void __launch_bounds__(NT, 2) k_fused_rhs(const InstDev<float>* __res
                                                      int ninst) {
   extern __shared__ __align__(16) unsigned char smr[];
   const int N = insts[0].N;
+  // this step's maxima of the Poisson source start from zero (fused_div records them)
+  if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0)
+    for (int i = threadIdx.x; i < 2 * ninst; i += blockDim.x) insts[i >> 1].wmax[i & 1] = 0;
   sweep_schedule<TX, TYR, PERSIST>(N, nchunk, zc, ninst, [&](int inst, int x0, int y0, int z0, int z1) {
     rhs_segment(insts[inst], par, N, x0, y0, z0, z1, smr);
   });
@@ -661,6 +664,7 @@ __device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, in
   float2 rD1[USD], rD2[USD];  // [site]
 #pragma unroll
   for (int k = 0; k < USD; ++k) rD1[k] = rD2[k] = f2(0.f, 0.f);
+  float amx = 0.f, amy = 0.f;  // max |Re W|, |Im W| of this thread's outputs
   const float2 four = f2(4.f, 4.f);
 #pragma unroll
   for (int k = 0; k < DRD - 1; ++k) issue(k);
@@ -702,9 +706,15 @@ __device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, in
       const float2 dv = vadd(vadd(rD1[k], Q), zr);
       rD1[k] = vfma(four, Q, rD2[k]);
       rD2[k] = vsub(Q, zr);
-      if (i >= 2) oW[(size_t)(z0 - 2 + i) * NN + gc0 + (size_t)k * N] = vmul(vsplat(kd, float2()), dv);
+      if (i >= 2) {
+        const float2 wv = vmul(vsplat(kd, float2()), dv);
+        oW[(size_t)(z0 - 2 + i) * NN + gc0 + (size_t)k * N] = wv;
+        amx = fmaxf(amx, fabsf(wv.x));
+        amy = fmaxf(amy, fabsf(wv.y));
+      }
     }
   }
+  record_wmax(I.wmax, amx, amy);
 }
 
 template <bool PERSIST>
@@ -721,6 +731,8 @@ __device__ __forceinline__ void correct_segment(const InstDev<float>& I, int par
                                                 unsigned char* smc) {
   const float kd = I.ph.c2h * (1.f / 36.f);
   const float dt = I.ph.dt;
+  // the pressures come out of the FFT scaled by powers of two (pow2_norm): undo it, exactly
+  const float du = pow2_denorm(I.wmax[0]), dp = pow2_denorm(I.wmax[1]);
   const size_t NN = (size_t)N * N;
   const int niter = (z1 - z0) + 2;
   const float* qs[6] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2],
@@ -798,8 +810,8 @@ __device__ __forceinline__ void correct_segment(const InstDev<float>& I, int par
       const float gv[3] = {gx.x, gy.x, gz.x}, gp[3] = {gx.y, gy.y, gz.y};
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
-        oU[b][g] = qc[b * CN] - dt * (kd * gv[b]);
-        oP[b][g] = qc[(3 + b) * CN] - dt * (kd * gp[b]);
+        oU[b][g] = qc[b * CN] - dt * (kd * (gv[b] * du));
+        oP[b][g] = qc[(3 + b) * CN] - dt * (kd * (gp[b] * dp));
       }
     }
   }

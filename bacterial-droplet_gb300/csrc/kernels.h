@@ -72,9 +72,10 @@ void fused_prepare();
 
 // readDraw.py reductions (post.cu): centroid partials (centroid_blocks() x 4 doubles) and the
 // 9 slice planes of N*N doubles at z = zs.
-// FP64 <-> FP32 field conversion on the device (post.cu): dst[i] = src[i] and dst[i] = src[i * stride].
+// FP64 <-> FP32 field conversion on the device (post.cu): dst[i] = src[i] and
+// dst[i] = src[i * stride] * scale (an exact power of two).
 void launch_to_f32(const double* src, float* dst, size_t n, cudaStream_t st);
-void launch_to_f64(const float* src, size_t stride, double* dst, size_t n, cudaStream_t st);
+void launch_to_f64(const float* src, size_t stride, double* dst, size_t n, double scale, cudaStream_t st);
 int centroid_blocks();
 template <class T> void launch_centroid(const InstDev<T>* d_all, int inst, int par, double* part, cudaStream_t st);
 template <class T>

@@ -40,6 +40,9 @@ __global__ void __launch_bounds__(BX* BY) k_stage1(const InstDev<T>* __restrict_
   const InstDev<T>& I = insts[blockIdx.z / N];
   const int z = blockIdx.z % N;
   const int x = blockIdx.x * BX + threadIdx.x, y = blockIdx.y * BY + threadIdx.y;
+  // FP32: this step's maxima of the Poisson source start from zero (k_div records them)
+  if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.y == 0 && I.wmax)
+    for (int i = threadIdx.x; i < 2 * (int)(gridDim.z / N); i += blockDim.x) insts[i >> 1].wmax[i & 1] = 0;
   if (x >= N || y >= N) return;
   Site s;
   s.init(x, y, z, N);
@@ -155,6 +158,7 @@ __global__ void __launch_bounds__(BX* BY) k_div(const InstDev<T>* __restrict__ i
   w.x = d[0];
   w.y = d[1];
   I.W[s.idx] = w;
+  if constexpr (sizeof(T) == 4) record_wmax(I.wmax, d[0], d[1]);
 }
 
 template <class T>
@@ -170,13 +174,19 @@ __global__ void __launch_bounds__(BX* BY) k_correct(const InstDev<T>* __restrict
   const T* W = reinterpret_cast<const T*>(I.W);
   Acc<T> Fv = s.acc<T>(W, 2), Fp = s.acc<T>(W + 1, 2);
   const int i = s.idx;
+  // FP32: the pressures come out of the FFT scaled by powers of two (pow2_norm); undo it exactly
+  T du = T(1), dp = T(1);
+  if constexpr (sizeof(T) == 4) {
+    du = pow2_denorm(I.wmax[0]);
+    dp = pow2_denorm(I.wmax[1]);
+  }
   // getVNew (TTSH3D.cu:505-511)
-  I.U[0][i] = I.Us[par ^ 1][0][i] - p.dt * st_dx<T>(Fv, p.c2h);
-  I.U[1][i] = I.Us[par ^ 1][1][i] - p.dt * st_dy<T>(Fv, p.c2h);
-  I.U[2][i] = I.Us[par ^ 1][2][i] - p.dt * st_dz<T>(Fv, p.c2h);
-  I.P[0][i] = I.Ps[par ^ 1][0][i] - p.dt * st_dx<T>(Fp, p.c2h);
-  I.P[1][i] = I.Ps[par ^ 1][1][i] - p.dt * st_dy<T>(Fp, p.c2h);
-  I.P[2][i] = I.Ps[par ^ 1][2][i] - p.dt * st_dz<T>(Fp, p.c2h);
+  I.U[0][i] = I.Us[par ^ 1][0][i] - p.dt * (st_dx<T>(Fv, p.c2h) * du);
+  I.U[1][i] = I.Us[par ^ 1][1][i] - p.dt * (st_dy<T>(Fv, p.c2h) * du);
+  I.U[2][i] = I.Us[par ^ 1][2][i] - p.dt * (st_dz<T>(Fv, p.c2h) * du);
+  I.P[0][i] = I.Ps[par ^ 1][0][i] - p.dt * (st_dx<T>(Fp, p.c2h) * dp);
+  I.P[1][i] = I.Ps[par ^ 1][1][i] - p.dt * (st_dy<T>(Fp, p.c2h) * dp);
+  I.P[2][i] = I.Ps[par ^ 1][2][i] - p.dt * (st_dz<T>(Fp, p.c2h) * dp);
 }
 
 constexpr int STATS_BLOCKS = 256, STATS_THREADS = 256;

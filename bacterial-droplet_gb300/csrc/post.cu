@@ -85,9 +85,9 @@ __global__ void k_to_f32(const double* __restrict__ src, float* __restrict__ dst
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     dst[i] = __double2float_rn(src[i]);
 }
-__global__ void k_to_f64(const float* __restrict__ src, size_t stride, double* __restrict__ dst, size_t n) {
+__global__ void k_to_f64(const float* __restrict__ src, size_t stride, double* __restrict__ dst, size_t n, double scale) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    dst[i] = (double)src[i * stride];
+    dst[i] = (double)src[i * stride] * scale;
 }
 
 }  // namespace
@@ -97,8 +97,8 @@ void launch_to_f32(const double* src, float* dst, size_t n, cudaStream_t st) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) throw std::runtime_error(std::string("conversion launch: ") + cudaGetErrorString(e));
 }
-void launch_to_f64(const float* src, size_t stride, double* dst, size_t n, cudaStream_t st) {
-  k_to_f64<<<1216, 256, 0, st>>>(src, stride, dst, n);
+void launch_to_f64(const float* src, size_t stride, double* dst, size_t n, double scale, cudaStream_t st) {
+  k_to_f64<<<1216, 256, 0, st>>>(src, stride, dst, n, scale);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) throw std::runtime_error(std::string("conversion launch: ") + cudaGetErrorString(e));
 }
