@@ -301,8 +301,11 @@ void build_engine(ttsh_sim* s, Engine<T>& E) {
     const int N = ih.N;
     const size_t nn = (size_t)N * N * N;
     const size_t fb = align256(nn * sizeof(T));
+    // phi x2, P, u, u* x2, P* x2, the packed Poisson field W, and: fused, the phi compensation and
+    // the bf16 compensations of u, P (6) and of u*, P* x2 (12); plain, the 13 intermediates
     const int nfields = 2 + 3 + 3 + 6 + 6 + (s->fused ? 1 : 13);
-    const size_t bytes = nfields * fb + align256(nn * sizeof(C));
+    const size_t lb = align256(nn * sizeof(__nv_bfloat16));
+    const size_t bytes = nfields * fb + align256(nn * sizeof(C)) + (s->fused ? 18 * lb : 0);
     char* d = nullptr;
     cudaError_t e = cudaMalloc(&d, bytes);
     if (e != cudaSuccess) throw std::bad_alloc();
@@ -326,7 +329,13 @@ void build_engine(ttsh_sim* s, Engine<T>& E) {
       for (int b = 0; b < 3; ++b) I.Us[q][b] = take();
     for (int q = 0; q < 2; ++q)
       for (int b = 0; b < 3; ++b) I.Ps[q][b] = take();
-    if (s->fused) I.phic = take();
+    if (s->fused) {
+      I.phic = take();
+      auto take_b = [&]() { __nv_bfloat16* p = reinterpret_cast<__nv_bfloat16*>(d + off); off += lb; return p; };
+      for (int f = 0; f < 6; ++f) I.lo[f] = take_b();
+      for (int q = 0; q < 2; ++q)
+        for (int f = 0; f < 6; ++f) I.slo[q][f] = take_b();
+    }
     if (!s->fused) {
       I.mu0 = take();
       for (int b = 0; b < 3; ++b) I.mu[b] = take();
@@ -335,12 +344,16 @@ void build_engine(ttsh_sim* s, Engine<T>& E) {
     I.W = reinterpret_cast<C*>(d + off);
   }
   if constexpr (std::is_same<T, float>::value) {
-    // the per-droplet maxima of the packed Poisson source (two ints each), for its balancing
+    // per droplet: the maxima of the packed Poisson source (two ints, for its balancing) and, in
+    // the fused form, of u*, P* (two ints, the grid of the exact divergence)
     int* wm = nullptr;
-    CK(cudaMalloc(&wm, 2 * sizeof(int) * (size_t)n));
-    CK(cudaMemset(wm, 0, 2 * sizeof(int) * (size_t)n));
+    CK(cudaMalloc(&wm, 4 * sizeof(int) * (size_t)n));
+    CK(cudaMemset(wm, 0, 4 * sizeof(int) * (size_t)n));
     s->tables.push_back(wm);
-    for (int i = 0; i < n; ++i) E.h[i].wmax = wm + 2 * i;
+    for (int i = 0; i < n; ++i) {
+      E.h[i].wmax = wm + 4 * i;
+      if (s->fused) E.h[i].smax = wm + 4 * i + 2;
+    }
   }
   if (!s->d_err) {
     CK(cudaMalloc(&s->d_err, sizeof(int)));
@@ -602,6 +615,10 @@ struct TrialBackup {
       if (I.phic) arrays.push_back({I.phic, n * sizeof(T)});
       arrays.push_back({I.W, 2 * n * sizeof(T)});
       if (I.wmax) arrays.push_back({I.wmax, 2 * sizeof(int)});  // the pressures' scales
+      if (I.smax) {  // the fused form's compensations of u, P and the grid of its next divergence
+        arrays.push_back({I.smax, 2 * sizeof(int)});
+        for (int f = 0; f < 6; ++f) arrays.push_back({I.lo[f], n * sizeof(__nv_bfloat16)});
+      }
     }
     size_t tot = 0;
     for (auto& a : arrays) tot += a.second;
@@ -788,16 +805,24 @@ static double* conv_scratch(const ttsh_sim* s, const I_& I) {
   else return nullptr;
 }
 
-// The 13 state arrays of a checkpoint, in file order, as device pointers of the current parity.
+// The state arrays of a checkpoint, in file order, as (device pointer, bytes) of the current
+// parity: phi, P, u, u*, P* of the element type, and in the fused form then the phi compensation
+// and the bf16 compensations of u, P and of u*, P* (everything the next step reads).
 template <class E>
-static std::vector<void*> state_arrays(ttsh_sim* s, E& eng, int inst) {
+static std::vector<std::pair<void*, size_t>> state_arrays(ttsh_sim* s, E& eng, int inst) {
   auto& I = eng.h[inst];
-  std::vector<void*> a = {I.phi[s->par]};
-  for (int b = 0; b < 3; ++b) a.push_back(I.P[b]);
-  for (int b = 0; b < 3; ++b) a.push_back(I.U[b]);
-  for (int b = 0; b < 3; ++b) a.push_back(I.Us[s->par][b]);
-  for (int b = 0; b < 3; ++b) a.push_back(I.Ps[s->par][b]);
-  if (I.phic) a.push_back(I.phic);  // fused form: the phi-update compensation (14th array)
+  typedef typename std::decay<decltype(*I.phi[0])>::type TT;
+  const size_t n = (size_t)I.N * I.N * I.N, es = sizeof(TT), eb = sizeof(__nv_bfloat16);
+  std::vector<std::pair<void*, size_t>> a = {{I.phi[s->par], n * es}};
+  for (int b = 0; b < 3; ++b) a.push_back({I.P[b], n * es});
+  for (int b = 0; b < 3; ++b) a.push_back({I.U[b], n * es});
+  for (int b = 0; b < 3; ++b) a.push_back({I.Us[s->par][b], n * es});
+  for (int b = 0; b < 3; ++b) a.push_back({I.Ps[s->par][b], n * es});
+  if (I.phic) {
+    a.push_back({I.phic, n * es});
+    for (int f = 0; f < 6; ++f) a.push_back({I.lo[f], n * eb});
+    for (int f = 0; f < 6; ++f) a.push_back({I.slo[s->par][f], n * eb});
+  }
   return a;
 }
 
@@ -939,6 +964,33 @@ int ttsh_set_state(ttsh_sim* s, int inst, const double* phi, const double* P, co
     CK(cudaStreamSynchronize(s->stream));
     const int N = s->inst[inst].N;
     const size_t n = (size_t)N * N * N;
+    if (s->fused) {
+      // compensated fields: FP32 value + remainder; no grid for the first divergence yet
+      InstDev<float>& I = s->ef.h[inst];
+      double* scr = conv_scratch(s, I);
+      auto put = [&](const double* src, float* hi, __nv_bfloat16* lo, float* lo32) {
+        CK(cudaMemcpyAsync(scr, src, n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+        launch_split(scr, hi, lo, lo32, n, s->stream);
+      };
+      put(phi, I.phi[s->par], nullptr, I.phic);
+      for (int b = 0; b < 3; ++b) {
+        put(u + b * n, I.U[b], I.lo[b], nullptr);
+        put(P + b * n, I.P[b], I.lo[3 + b], nullptr);
+        if (ustar) put(ustar + b * n, I.Us[s->par][b], I.slo[s->par][b], nullptr);
+        else {
+          CK(cudaMemsetAsync(I.Us[s->par][b], 0, n * sizeof(float), s->stream));
+          CK(cudaMemsetAsync(I.slo[s->par][b], 0, n * sizeof(__nv_bfloat16), s->stream));
+        }
+        if (Pstar) put(Pstar + b * n, I.Ps[s->par][b], I.slo[s->par][3 + b], nullptr);
+        else {
+          CK(cudaMemsetAsync(I.Ps[s->par][b], 0, n * sizeof(float), s->stream));
+          CK(cudaMemsetAsync(I.slo[s->par][3 + b], 0, n * sizeof(__nv_bfloat16), s->stream));
+        }
+      }
+      CK(cudaMemsetAsync(I.smax, 0, 2 * sizeof(int), s->stream));
+      CK(cudaStreamSynchronize(s->stream));
+      return TTSH_OK;
+    }
     s->with_engine([&](auto& E) {
       auto& I = E.h[inst];
       typedef typename std::decay<decltype(*I.phi[0])>::type TT;
@@ -994,10 +1046,25 @@ int ttsh_get_state(ttsh_sim* s, int inst, double* phi, double* P, double* u, dou
       auto& I = E.h[inst];
       typedef typename std::decay<decltype(*I.phi[0])>::type TT;
       double* scr = conv_scratch(s, I);
-      if (phi) d2h<TT>(phi, I.phi[s->par], n, s->stream, scr);
-      for (int b = 0; b < 3; ++b) {
-        if (P) d2h<TT>(P + b * n, I.P[b], n, s->stream, scr);
-        if (u) d2h<TT>(u + b * n, I.U[b], n, s->stream, scr);
+      if constexpr (std::is_same<TT, float>::value) {
+        if (s->fused) {  // the compensated values
+          auto get = [&](double* dst, const float* hi, const __nv_bfloat16* lo, const float* lo32) {
+            launch_join(hi, lo, lo32, scr, n, s->stream);
+            CK(cudaMemcpyAsync(dst, scr, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+          };
+          if (phi) get(phi, I.phi[s->par], nullptr, I.phic);
+          for (int b = 0; b < 3; ++b) {
+            if (P) get(P + b * n, I.P[b], I.lo[3 + b], nullptr);
+            if (u) get(u + b * n, I.U[b], I.lo[b], nullptr);
+          }
+        }
+      }
+      if (!s->fused) {
+        if (phi) d2h<TT>(phi, I.phi[s->par], n, s->stream, scr);
+        for (int b = 0; b < 3; ++b) {
+          if (P) d2h<TT>(P + b * n, I.P[b], n, s->stream, scr);
+          if (u) d2h<TT>(u + b * n, I.U[b], n, s->stream, scr);
+        }
       }
       const TT* w = reinterpret_cast<const TT*>(I.W);
       double sv = 1.0, sp = 1.0;  // FP32: the pressures' power-of-two scales (pow2_norm, common.cuh)
@@ -1027,9 +1094,23 @@ int ttsh_get_provisional(ttsh_sim* s, int inst, double* ustar, double* Pstar) {
     s->with_engine([&](auto& E) {
       auto& I = E.h[inst];
       typedef typename std::decay<decltype(*I.phi[0])>::type TT;
+      double* scr = conv_scratch(s, I);
       for (int b = 0; b < 3; ++b) {
-        if (ustar) d2h<TT>(ustar + b * n, I.Us[s->par][b], n, s->stream, conv_scratch(s, I));
-        if (Pstar) d2h<TT>(Pstar + b * n, I.Ps[s->par][b], n, s->stream, conv_scratch(s, I));
+        if constexpr (std::is_same<TT, float>::value) {
+          if (s->fused) {  // the last step's u*, P*, compensated
+            if (ustar) {
+              launch_join(I.Us[s->par][b], I.slo[s->par][b], nullptr, scr, n, s->stream);
+              CK(cudaMemcpyAsync(ustar + b * n, scr, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+            }
+            if (Pstar) {
+              launch_join(I.Ps[s->par][b], I.slo[s->par][3 + b], nullptr, scr, n, s->stream);
+              CK(cudaMemcpyAsync(Pstar + b * n, scr, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+            }
+            continue;
+          }
+        }
+        if (ustar) d2h<TT>(ustar + b * n, I.Us[s->par][b], n, s->stream, scr);
+        if (Pstar) d2h<TT>(Pstar + b * n, I.Ps[s->par][b], n, s->stream, scr);
       }
       CK(cudaStreamSynchronize(s->stream));
     });
@@ -1290,6 +1371,8 @@ int ttsh_run_dirs(const char* const* dirs, int n, const ttsh_ext* ext, uint64_t 
 
 static const char kCkpMagic[8] = {'T', 'T', 'S', 'H', 'C', 'K', 'P', '1'};
 
+// Checkpoint file: "TTSHCKP1", int32 {1, N, precision, arrays beyond the first 13}, FP64 T, int64
+// steps, then the state arrays (state_arrays) as raw device bytes.
 int ttsh_save_checkpoint(ttsh_sim* s, int inst, const char* path) {
   int rc = check_inst(s, inst);
   if (rc) return rc;
@@ -1298,21 +1381,21 @@ int ttsh_save_checkpoint(ttsh_sim* s, int inst, const char* path) {
     CK(cudaSetDevice(s->device));
     CK(cudaStreamSynchronize(s->stream));
     const int N = s->inst[inst].N;
-    const size_t n = (size_t)N * N * N, es = s->precision == 32 ? 4 : 8;
     FILE* fp = std::fopen(path, "wb");
     if (!fp) return set_error(TTSH_E_IO, std::string("cannot open ") + path);
-    std::vector<void*> arr;
+    std::vector<std::pair<void*, size_t>> arr;
     s->with_engine([&](auto& E) { arr = state_arrays(s, E, inst); });
     int32_t hdr[4] = {1, N, s->precision, (int32_t)arr.size() - 13};
     double T = s->inst[inst].T;
     int64_t steps = s->steps;
     bool ok = std::fwrite(kCkpMagic, 1, 8, fp) == 8 && std::fwrite(hdr, 4, 4, fp) == 4 &&
               std::fwrite(&T, 8, 1, fp) == 1 && std::fwrite(&steps, 8, 1, fp) == 1;
-    std::vector<char> buf(n * es);
-    for (void* d : arr) {
+    std::vector<char> buf;
+    for (const auto& a : arr) {
       if (!ok) break;
-      CK(cudaMemcpy(buf.data(), d, n * es, cudaMemcpyDeviceToHost));
-      ok = std::fwrite(buf.data(), 1, n * es, fp) == n * es;
+      buf.resize(a.second);
+      CK(cudaMemcpy(buf.data(), a.first, a.second, cudaMemcpyDeviceToHost));
+      ok = std::fwrite(buf.data(), 1, a.second, fp) == a.second;
     }
     if (std::fclose(fp) != 0) ok = false;
     return ok ? TTSH_OK : set_error(TTSH_E_IO, std::string("write failed: ") + path);
@@ -1327,7 +1410,6 @@ int ttsh_load_checkpoint(ttsh_sim* s, int inst, const char* path) {
     CK(cudaSetDevice(s->device));
     CK(cudaStreamSynchronize(s->stream));
     const int N = s->inst[inst].N;
-    const size_t n = (size_t)N * N * N, es = s->precision == 32 ? 4 : 8;
     FILE* fp = std::fopen(path, "rb");
     if (!fp) return set_error(TTSH_E_IO, std::string("cannot open ") + path);
     char magic[8];
@@ -1340,19 +1422,20 @@ int ttsh_load_checkpoint(ttsh_sim* s, int inst, const char* path) {
       std::fclose(fp);
       return set_error(TTSH_E_PARSE, std::string("not a ttsh checkpoint: ") + path);
     }
-    std::vector<void*> arr;
+    std::vector<std::pair<void*, size_t>> arr;
     s->with_engine([&](auto& E) { arr = state_arrays(s, E, inst); });
     if (hdr[1] != N || hdr[2] != s->precision || hdr[3] != (int32_t)arr.size() - 13) {
       std::fclose(fp);
       return set_error(TTSH_E_INVALID, "checkpoint size, precision or form differs from the instance");
     }
-    std::vector<char> buf(n * es);
-    for (void* d : arr) {
-      if (std::fread(buf.data(), 1, n * es, fp) != n * es) {
+    std::vector<char> buf;
+    for (const auto& a : arr) {
+      buf.resize(a.second);
+      if (std::fread(buf.data(), 1, a.second, fp) != a.second) {
         std::fclose(fp);
         return set_error(TTSH_E_PARSE, std::string("truncated checkpoint: ") + path);
       }
-      CK(cudaMemcpy(d, buf.data(), n * es, cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(a.first, buf.data(), a.second, cudaMemcpyHostToDevice));
     }
     std::fclose(fp);
     s->inst[inst].T = T;

@@ -1,6 +1,7 @@
 // common.cuh — shared device types of libttsh: per-droplet descriptors and the
 // reference-order stencils of TTSH3D.cu (d1{x,y,z}CO2I3D, laplaceCO2I3D, :3280-3343).
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -43,6 +44,11 @@ struct InstDev {
   T* phic;            // fused form: compensation of the phi update (the low part lost to rounding)
   int* wmax;          // FP32 forms: max |Re W|, max |Im W| of this step's Poisson source (float bits,
                       // non-negative floats order as ints); null in the FP64 form
+  // Fused FP32 form only (null elsewhere): u, P and the u*, P* ping-pong stored compensated, the
+  // FP32 value (U, P, Us, Ps) plus, in bf16, the part of the exact value its rounding dropped
+  __nv_bfloat16* lo[6];      // u (0..2), P (3..5)
+  __nv_bfloat16* slo[2][6];  // u*, P* of parity q
+  int* smax;                 // max |u*|, max |P*| of this step (float bits): the divergence's grid
   T* mu0;             // plain-form intermediates
   T* mu[3];
   T* sig[9];          // sig[a*3+b] = phi * D_a P_b
@@ -83,8 +89,8 @@ __host__ __device__ inline float pow2_denorm(int mbits) {
   memcpy(&s, &bits, sizeof s);
   return s;
 }
-// Warp-aggregated record of the source's maxima |Re|, |Im| (float bits) into wmax[0..1]; any
-// subset of a warp's lanes may call it.
+// Warp-aggregated record of two maxima |a|, |b| (float bits) into dst[0..1] (the Poisson source's
+// parts, the provisional fields); any subset of a warp's lanes may call it.
 __device__ __forceinline__ void record_wmax(int* wmax, float ax, float ay) {
   const unsigned act = __activemask();
   const unsigned mx = __reduce_max_sync(act, __float_as_uint(fabsf(ax)));

@@ -9,6 +9,12 @@
 //                 the reference's stale halo for neighbours across the periodic boundary)
 //   fused_correct u*, P*, W -> u, P   (getVNew, :505-511)
 //
+// u, P and u*, P* are stored compensated: the FP32 value, which the stencils read, and in bf16
+// the part of the exact value that FP32 rounding dropped, carried through every update (TwoSum).
+// The divergence that feeds the pressure is taken exactly from both (fused_div): u* is nearly
+// solenoidal, so its divergence is a small difference of large values, and 1/dt amplifies
+// whatever rounding it carries into the pressure.
+//
 // All three march along z through a tile of columns (a "2.5D" sweep; fused_rhs 32 x 8, fused_div
 // 32 x 32, fused_correct 32 x 16), on a chunked or a persistent schedule: each z-plane of
 // every field the stencils need is staged once in a shared-memory ring of planes, and each
@@ -176,6 +182,24 @@ __device__ __forceinline__ void sep_rows(const LD& ld, const SepK& k, V* dx, V* 
   }
 }
 
+// s + e = a + b exactly (Knuth's TwoSum: six FP32 additions, no assumption on the magnitudes).
+__device__ __forceinline__ float two_sum(float a, float b, float& e) {
+  const float s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+  return s;
+}
+
+// x* = x + d stored compensated: the FP32 sum and, in bf16, what its rounding dropped plus the
+// compensation x_lo that x brought along. Returns the FP32 value.
+__device__ __forceinline__ float put_comp(float* hi, __nv_bfloat16* lo, size_t g, float x, float d, __nv_bfloat16 x_lo) {
+  float e;
+  const float s = two_sum(x, d, e);
+  hi[g] = s;
+  lo[g] = __float2bfloat16_rn(e + __bfloat162float(x_lo));
+  return s;
+}
+
 // ------------------------------------------------------------------------------------------
 // One segment of the sweep: the tile column (x0, y0) of droplet I, output planes z0 .. z1 - 1.
 __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, int N, int x0, int y0, int z0, int z1,
@@ -188,6 +212,8 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
   const float* __restrict__ gU[3] = {I.U[0], I.U[1], I.U[2]};
   float* const oUs[3] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2]};
   float* const oPs[3] = {I.Ps[par ^ 1][0], I.Ps[par ^ 1][1], I.Ps[par ^ 1][2]};
+  __nv_bfloat16* const* oSlo = I.slo[par ^ 1];
+  float amu = 0.f, amp = 0.f;  // max |u*|, |P*| of this thread's outputs (the divergence's grid)
   float* const ophi = I.phi[par ^ 1];
   float* const phic = I.phic;
   float2* const sA = reinterpret_cast<float2*>(smr + OFF_A);      // [RA][2][ANP]: (phi, Px), (Py, Pz)
@@ -275,12 +301,25 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
     cp_async_wait_all();
     __syncthreads();
     if (i + 1 < niter) issue(i + 1);
-    // the phi compensation of this iteration's output sites (half A), loaded before phase 1 so
-    // that the phase-1 work covers the load
+    // the compensations of this iteration's output sites (phi, u_x and P in half A; u_y, u_z in
+    // half B), loaded before phase 1 so that the phase-1 work covers the loads
     float cprev[2] = {0.f, 0.f};
-    if (i >= 4 && halfA) {
+    __nv_bfloat16 lprev[2][4];
+    if (i >= 4) {
 #pragma unroll
-      for (int k = 0; k < 2; ++k) cprev[k] = phic[(size_t)(z0 - 4 + i) * NN + (size_t)(y0 + py0 + k) * N + (x0 + px)];
+      for (int k = 0; k < 2; ++k) {
+        const size_t g = (size_t)(z0 - 4 + i) * NN + (size_t)(y0 + py0 + k) * N + (x0 + px);
+        if (halfA) {
+          cprev[k] = phic[g];
+          lprev[k][0] = I.lo[0][g];
+          lprev[k][1] = I.lo[3][g];
+          lprev[k][2] = I.lo[4][g];
+          lprev[k][3] = I.lo[5][g];
+        } else {
+          lprev[k][0] = I.lo[1][g];
+          lprev[k][1] = I.lo[2][g];
+        }
+      }
     }
     // ---- phase 1a, stage 1 at plane b = z0 - 3 + i over B (tile+1): the products mu_0, mu_b,
     //      S_ab that phase 2 differentiates, and on the tile the pointwise parts of the update
@@ -480,12 +519,15 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
             const float2 q0 = pq[0 * CNP + c], q1 = pq[1 * CNP + c], q2 = pq[2 * CNP + c], q3 = pq[3 * CNP + c];
             const float2 A0 = ac[oa], A1 = ac[ANP + oa];
             // u*_x = u_x + dt d/dt u_x (:480-482)
-            oUs[0][g] = fmaf(p.dt, fmaf(sk.d, dvx[k], q0.x), sU01[sl * BNP + ob].x);
+            const float usx = put_comp(oUs[0], oSlo[0], g, sU01[sl * BNP + ob].x, p.dt * fmaf(sk.d, dvx[k], q0.x),
+                                       lprev[k][0]);
             // P*_b = P_b + dt (pointwise part + eta L mu_b) (:623-629, :486-488)
-            oPs[0][g] = fmaf(p.dt, fmaf(p.eta, lm[k][0].y, q2.x), A0.y);
-            const float2 ps2 = vfma(vsplat(p.dt, float2()), vfma(vsplat(p.eta, float2()), lm[k][1], f2(q2.y, q3.x)), A1);
-            oPs[1][g] = ps2.x;
-            oPs[2][g] = ps2.y;
+            const float psx = put_comp(oPs[0], oSlo[3], g, A0.y, p.dt * fmaf(p.eta, lm[k][0].y, q2.x), lprev[k][1]);
+            const float2 dp2 = vmul(vsplat(p.dt, float2()), vfma(vsplat(p.eta, float2()), lm[k][1], f2(q2.y, q3.x)));
+            const float psy = put_comp(oPs[1], oSlo[4], g, A1.x, dp2.x, lprev[k][2]);
+            const float psz = put_comp(oPs[2], oSlo[5], g, A1.y, dp2.y, lprev[k][3]);
+            amu = fmaxf(amu, fabsf(usx));
+            amp = fmaxf(amp, fmaxf(fabsf(psx), fmaxf(fabsf(psy), fabsf(psz))));
             // phi' = phi + dt (-u.D phi + gamma L mu_0) (:631, :515), compensated: the part of
             // the increment that rounding drops from phi is carried to the next step (otherwise
             // increments below half an ulp of phi are lost, a systematic mass drift)
@@ -538,15 +580,16 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
             const size_t g = (size_t)zc * NN + (size_t)(y0 + py0 + k) * N + (x0 + px);
             const float2 q0 = pq[0 * CNP + c], q1 = pq[1 * CNP + c];
             // (u*_y, u*_z) = (u_y, u_z) + dt d/dt (u_y, u_z) (:480-482)
-            const float2 us = vfma(vsplat(p.dt, float2()), vfma(vsplat(sk.d, float2()), dv[k], f2(q0.y, q1.x)),
-                                   f2(sU01[sl * BNP + ob].y, sU2[sl * BNP + ob]));
-            oUs[1][g] = us.x;
-            oUs[2][g] = us.y;
+            const float2 du = vmul(vsplat(p.dt, float2()), vfma(vsplat(sk.d, float2()), dv[k], f2(q0.y, q1.x)));
+            const float usy = put_comp(oUs[1], oSlo[1], g, sU01[sl * BNP + ob].y, du.x, lprev[k][0]);
+            const float usz = put_comp(oUs[2], oSlo[2], g, sU2[sl * BNP + ob], du.y, lprev[k][1]);
+            amu = fmaxf(amu, fmaxf(fabsf(usy), fabsf(usz)));
           }
         }
       }
     }
   }
+  record_wmax(I.smax, amu, amp);
 }
 
 // The two schedules of the three fused kernels. zc > 0: CTA (bx, by, bz) sweeps tile (bx, by)
@@ -595,9 +638,14 @@ constexpr int SW = TX + 8;              // fused_div row, floats x0 - 4 .. x0 + 
 constexpr int CW = TX + 4;              // fused_correct row, float2 x0 - 2 .. x0 + TX + 1
 constexpr int CPL = CW * SH;            // float2 per staged plane
 constexpr int DR = 4;                   // ring slots of fused_correct
-// fused_div: a taller tile (TX x TYD) and a 3-slot ring (2 planes in flight)
-constexpr int TYD = 32, SHD = TYD + 2, SPLD = SW * SHD, DRD = 3;
-constexpr size_t DIV_SMEM = DRD * 6 * SPLD * sizeof(float);
+// fused_div: a taller tile (TX x TYD) and a 2-slot ring (1 plane in flight); each slot holds the
+// FP32 values of u*, P* and their bf16 compensations (rows x0 - 8 .. x0 + TX + 7, 16-byte chunks)
+constexpr int TYD = 32, SHD = TYD + 2, SPLD = SW * SHD, DRD = 2;
+constexpr int SWB = TX + 16, SPLB = SWB * SHD;
+constexpr size_t DIV_SLOT = 6 * SPLD * sizeof(float) + 6 * SPLB * sizeof(__nv_bfloat16);
+constexpr size_t DIV_SMEM = DRD * DIV_SLOT;
+static_assert((6 * SPLD * sizeof(float)) % 16 == 0 && DIV_SLOT % 16 == 0, "16-byte aligned staging");
+static_assert(2 * DIV_SMEM <= 227 * 1024, "fused_div: two CTAs per SM");
 constexpr size_t COR_SLOT = CPL * sizeof(float2) + 6 * CN * sizeof(float);  // p_v, p_p on B; u*, P* on C
 constexpr size_t COR_SMEM = DR * COR_SLOT;
 
@@ -619,40 +667,65 @@ __device__ __forceinline__ void cp_async_wait_div() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(DRD - 2) : "memory");
 }
 
+// The grid of the exact part of the divergence: S = 1.5 * 2^(E + 7) with 2^E >= 2 max |v| (float
+// bits of max |v|, 0: none). (v + S) - S rounds v to a multiple of g = 2^(E - 16), exactly, and the
+// divergence's separable sums of such values (at most 216 x 2^16 g) stay exact in FP32.
+__device__ __forceinline__ float split_grid(int mbits) {
+  int e = mbits > 0 ? ((mbits >> 23) & 0xff) - 127 + 2 : -100;
+  e = e < -120 ? -120 : (e > 110 ? 110 : e);
+  return __int_as_float(((127 + e + 7) << 23) | 0x400000);
+}
+
 __device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, int N, int x0, int y0, int z0, int z1,
-                                            float* sm) {
+                                            unsigned char* sm) {
   const size_t NN = (size_t)N * N;
   const float* cur[6] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2],
                          I.Ps[par ^ 1][0], I.Ps[par ^ 1][1], I.Ps[par ^ 1][2]};
   const float* old[6] = {I.Us[par][0], I.Us[par][1], I.Us[par][2], I.Ps[par][0], I.Ps[par][1], I.Ps[par][2]};
+  const __nv_bfloat16* const* curl = I.slo[par ^ 1];
+  const __nv_bfloat16* const* oldl = I.slo[par];
   float2* const oW = I.W;
   const int stale_q2 = I.stale;
   const float kd = I.ph.c2h * (1.f / 36.f) * I.ph.inv_dt;  // d/36 of the 27-point D, and 1/dt
+  const float2 S = f2(split_grid(I.smax[0]), split_grid(I.smax[1]));
   const int tid = threadIdx.x;
   const int niter = (z1 - z0) + 2;
+  auto slot_f = [&](int i) { return reinterpret_cast<float*>(sm + (i % DRD) * DIV_SLOT); };
+  auto slot_b = [&](int i) {
+    return reinterpret_cast<__nv_bfloat16*>(sm + (i % DRD) * DIV_SLOT + 6 * SPLD * sizeof(float));
+  };
   // issue(i): plane z0 - 1 + i into slot i % DRD (an empty group past the last plane, so that
   // every iteration commits one). Chunks outside the domain come from the previous step's u*, P*
-  // when the stale-halo quirk is on (the chunk grid is aligned with 0 and N).
+  // when the stale-halo quirk is on (the chunk grids are aligned with 0 and N).
   auto issue = [&](int i) {
     if (i >= niter) { cp_async_commit(); return; }
     const int zu = z0 - 1 + i;
     const bool zw = zu < 0 || zu >= N;
     const int zz = wrapN(zu, N);
-    float* dst = sm + (i % DRD) * 6 * SPLD;
-    constexpr int CR = SW / 4;  // chunks per row
-    for (int t = tid; t < SHD * CR; t += NTV) {
-      const int ry = t / CR, rc = t - ry * CR;
-      const int gx = x0 - 4 + 4 * rc, gy = y0 - 1 + ry;
+    float* dst = slot_f(i);
+    __nv_bfloat16* dsb = slot_b(i);
+    constexpr int CR = SW / 4, CRB = SWB / 8;  // chunks per row
+    for (int t = tid; t < SHD * (CR + CRB); t += NTV) {
+      const bool lo = t >= SHD * CR;
+      const int tt = lo ? t - SHD * CR : t, cr = lo ? CRB : CR;
+      const int ry = tt / cr, rc = tt - ry * cr;
+      const int gx = lo ? x0 - 8 + 8 * rc : x0 - 4 + 4 * rc, gy = y0 - 1 + ry;
       const bool stale = stale_q2 && (zw || gx < 0 || gx >= N || gy < 0 || gy >= N);
       const size_t g = (size_t)zz * NN + (size_t)wrapN(gy, N) * N + wrapN(gx, N);
+      if (lo) {
 #pragma unroll
-      for (int f = 0; f < 6; ++f) cp_async16(dst + f * SPLD + ry * SW + 4 * rc, (stale ? old[f] : cur[f]) + g);
+        for (int f = 0; f < 6; ++f) cp_async16(dsb + f * SPLB + ry * SWB + 8 * rc, (stale ? oldl[f] : curl[f]) + g);
+      } else {
+#pragma unroll
+        for (int f = 0; f < 6; ++f) cp_async16(dst + f * SPLD + ry * SW + 4 * rc, (stale ? old[f] : cur[f]) + g);
+      }
     }
     cp_async_commit();
   };
   const int qx = tid % TX, qy0 = (tid / TX) * USD;
   const size_t gc0 = (size_t)(y0 + qy0) * N + (x0 + qx);
-  const int wbase = qy0 * SW + (qx + 3);  // staged index of window row 0 (site 0's row - 1), column x - 1
+  const int wbase = qy0 * SW + (qx + 3);    // staged FP32 index of window row 0, column x - 1
+  const int wbaseB = qy0 * SWB + (qx + 7);  // staged bf16 index of the same
   // column x sits at the even staged index qx + 4 (rows and planes have even lengths), so the
   // aligned pair holding it starts at column offset pb of the window and the third column is sc
   const bool odd = (qx & 1) != 0;
@@ -660,10 +733,15 @@ __device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, in
   static_assert(SW % 2 == 0 && SPLD % 2 == 0, "aligned column pairs in the staged rows");
   // the divergence D_x v_x + D_y v_y + D_z v_z of v = (u*, P*) (getStream mode 0, :664-670), each
   // D = d/36 delta s s: a plane adds Q = delta_x s_y v_x + s_x delta_y v_y with weight s_z =
-  // (1, 4, 1) and Z = s_x s_y v_z with weight delta_z = (-1, 0, 1) over planes c-1, c, c+1
-  float2 rD1[USD], rD2[USD];  // [site]
+  // (1, 4, 1) and Z = s_x s_y v_z with weight delta_z = (-1, 0, 1) over planes c-1, c, c+1.
+  // It is taken in two parts, exactly: v = q + s with q the FP32 value rounded to the grid of
+  // split_grid, whose sums are exact, and s the rest (the FP32 value's remainder plus the bf16
+  // compensation), small enough that its sums' rounding is negligible. u* is nearly solenoidal,
+  // so its divergence is a small difference of large values; taken plainly in FP32 its rounding,
+  // amplified by 1/dt, would dominate the pressure.
+  float2 rD1[2][USD], rD2[2][USD];  // [part][site]
 #pragma unroll
-  for (int k = 0; k < USD; ++k) rD1[k] = rD2[k] = f2(0.f, 0.f);
+  for (int k = 0; k < USD; ++k) rD1[0][k] = rD2[0][k] = rD1[1][k] = rD2[1][k] = f2(0.f, 0.f);
   float amx = 0.f, amy = 0.f;  // max |Re W|, |Im W| of this thread's outputs
   const float2 four = f2(4.f, 4.f);
 #pragma unroll
@@ -672,8 +750,16 @@ __device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, in
     cp_async_wait_div();
     __syncthreads();
     issue(i + DRD - 1);  // into the slot read at iteration i - 1
-    const float* s = sm + (i % DRD) * 6 * SPLD + wbase;
-    auto w = [&](int comp, int r, int c) { return f2(s[comp * SPLD + r * SW + c], s[(3 + comp) * SPLD + r * SW + c]); };
+    const float* s = slot_f(i) + wbase;
+    const __nv_bfloat16* sb = slot_b(i) + wbaseB;
+    // value (u*, P*) of component comp at window row r, column c, split into (q, s)
+    auto split = [&](float2 hi, float2 lo, float2& q, float2& rest) {
+      q = vsub(vadd(hi, S), S);
+      rest = vadd(vsub(hi, q), lo);
+    };
+    auto lo2 = [&](int comp, int r, int c) {
+      return f2(__bfloat162float(sb[comp * SPLB + r * SWB + c]), __bfloat162float(sb[(3 + comp) * SPLB + r * SWB + c]));
+    };
     // the three columns x - 1, x, x + 1 of field f in window row r with two loads: the aligned
     // pair that holds x (x - 1, x for odd x; x, x + 1 for even x) and the remaining column
     auto row3 = [&](int f, int r, float& c0, float& c1, float& c2) {
@@ -684,30 +770,44 @@ __device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, in
       c1 = odd ? pr.y : pr.x;
       c2 = odd ? sv : pr.y;
     };
-    // per row of the window: the x-part delta_x v_x, and s_x of v_y and of v_z
-    float2 xd[USD + 2], ys[USD + 2], zs[USD + 2];
+    // per row of the window and part: the x-part delta_x v_x, and s_x of v_y and of v_z
+    float2 xd[2][USD + 2], ys[2][USD + 2], zs[2][USD + 2];
 #pragma unroll
     for (int r = 0; r < USD + 2; ++r) {
-      xd[r] = vsub(w(0, r, 2), w(0, r, 0));
-      float a0, a1, a2, b0, b1, b2;
-      row3(1, r, a0, a1, a2);
-      row3(4, r, b0, b1, b2);
-      ys[r] = vfma(four, f2(a1, b1), vadd(f2(a0, b0), f2(a2, b2)));
-      row3(2, r, a0, a1, a2);
-      row3(5, r, b0, b1, b2);
-      zs[r] = vfma(four, f2(a1, b1), vadd(f2(a0, b0), f2(a2, b2)));
+      float2 q0, s0, q2, s2;
+      split(f2(s[r * SW], s[3 * SPLD + r * SW]), lo2(0, r, 0), q0, s0);
+      split(f2(s[r * SW + 2], s[3 * SPLD + r * SW + 2]), lo2(0, r, 2), q2, s2);
+      xd[0][r] = vsub(q2, q0);
+      xd[1][r] = vsub(s2, s0);
+#pragma unroll
+      for (int comp = 1; comp <= 2; ++comp) {
+        float a[3], b[3];
+        row3(comp, r, a[0], a[1], a[2]);
+        row3(3 + comp, r, b[0], b[1], b[2]);
+        float2 qc[3], sc3[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) split(f2(a[c], b[c]), lo2(comp, r, c), qc[c], sc3[c]);
+        const float2 vq = vfma(four, qc[1], vadd(qc[0], qc[2]));
+        const float2 vs = vfma(four, sc3[1], vadd(sc3[0], sc3[2]));
+        if (comp == 1) { ys[0][r] = vq; ys[1][r] = vs; }
+        else { zs[0][r] = vq; zs[1][r] = vs; }
+      }
     }
 #pragma unroll
     for (int k = 0; k < USD; ++k) {
-      const float2 xr = vfma(four, xd[k + 1], vadd(xd[k], xd[k + 2]));  // delta_x s_y v_x
-      const float2 yr = vsub(ys[k + 2], ys[k]);                          // s_x delta_y v_y
-      const float2 zr = vfma(four, zs[k + 1], vadd(zs[k], zs[k + 2]));   // s_x s_y v_z
-      const float2 Q = vadd(xr, yr);
-      const float2 dv = vadd(vadd(rD1[k], Q), zr);
-      rD1[k] = vfma(four, Q, rD2[k]);
-      rD2[k] = vsub(Q, zr);
+      float2 dvp[2];
+#pragma unroll
+      for (int pt = 0; pt < 2; ++pt) {
+        const float2 xr = vfma(four, xd[pt][k + 1], vadd(xd[pt][k], xd[pt][k + 2]));  // delta_x s_y v_x
+        const float2 yr = vsub(ys[pt][k + 2], ys[pt][k]);                               // s_x delta_y v_y
+        const float2 zr = vfma(four, zs[pt][k + 1], vadd(zs[pt][k], zs[pt][k + 2]));    // s_x s_y v_z
+        const float2 Q = vadd(xr, yr);
+        dvp[pt] = vadd(vadd(rD1[pt][k], Q), zr);
+        rD1[pt][k] = vfma(four, Q, rD2[pt][k]);
+        rD2[pt][k] = vsub(Q, zr);
+      }
       if (i >= 2) {
-        const float2 wv = vmul(vsplat(kd, float2()), dv);
+        const float2 wv = vmul(vsplat(kd, float2()), vadd(dvp[0], dvp[1]));
         oW[(size_t)(z0 - 2 + i) * NN + gc0 + (size_t)k * N] = wv;
         amx = fmaxf(amx, fabsf(wv.x));
         amy = fmaxf(amy, fabsf(wv.y));
@@ -720,10 +820,10 @@ __device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, in
 template <bool PERSIST>
 __global__ void __launch_bounds__(NTV, 2) k_fused_div(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc,
                                                        int ninst) {
-  extern __shared__ __align__(16) float sm[];
+  extern __shared__ __align__(16) unsigned char smd[];
   const int N = insts[0].N;
   sweep_schedule<TX, TYD, PERSIST>(N, nchunk, zc, ninst, [&](int inst, int x0, int y0, int z0, int z1) {
-    div_segment(insts[inst], par, N, x0, y0, z0, z1, sm);
+    div_segment(insts[inst], par, N, x0, y0, z0, z1, smd);
   });
 }
 
@@ -778,6 +878,13 @@ __device__ __forceinline__ void correct_segment(const InstDev<float>& I, int par
 #pragma unroll
   for (int k = 0; k < DR - 1; ++k) issue(k);
   for (int i = 0; i < niter; ++i) {
+    // the compensations of u*, P* at this iteration's output site, loaded before the wait
+    __nv_bfloat16 sl[6];
+    if (i >= 2) {
+      const size_t g = (size_t)(z0 - 2 + i) * NN + gc;
+#pragma unroll
+      for (int f = 0; f < 6; ++f) sl[f] = I.slo[par ^ 1][f][g];
+    }
     cp_async_wait_ring();
     __syncthreads();
     issue(i + DR - 1);  // into the slot read at iteration i - 1
@@ -808,10 +915,11 @@ __device__ __forceinline__ void correct_segment(const InstDev<float>& I, int par
       const size_t g = (size_t)(z0 - 2 + i) * NN + gc;
       const float* qc = slot_q(i) + qy * TX + qx;
       const float gv[3] = {gx.x, gy.x, gz.x}, gp[3] = {gx.y, gy.y, gz.y};
+      // compensated: the FP32 value and, in bf16, what its rounding dropped plus u*'s compensation
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
-        oU[b][g] = qc[b * CN] - dt * (kd * (gv[b] * du));
-        oP[b][g] = qc[(3 + b) * CN] - dt * (kd * (gp[b] * dp));
+        put_comp(oU[b], I.lo[b], g, qc[b * CN], -(dt * (kd * (gv[b] * du))), sl[b]);
+        put_comp(oP[b], I.lo[3 + b], g, qc[(3 + b) * CN], -(dt * (kd * (gp[b] * dp))), sl[3 + b]);
       }
     }
   }
@@ -822,6 +930,10 @@ __global__ void __launch_bounds__(NTC, 2) k_fused_correct(const InstDev<float>* 
                                                           int zc, int ninst) {
   extern __shared__ __align__(16) unsigned char smc[];
   const int N = insts[0].N;
+  // the next step's maxima of u*, P* start from zero (fused_rhs records them; fused_div, which
+  // reads them, ran before this kernel)
+  if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0)
+    for (int i = threadIdx.x; i < 2 * ninst; i += blockDim.x) insts[i >> 1].smax[i & 1] = 0;
   sweep_schedule<TX, TY, PERSIST>(N, nchunk, zc, ninst, [&](int inst, int x0, int y0, int z0, int z1) {
     correct_segment(insts[inst], par, N, x0, y0, z0, z1, smc);
   });

@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(CT) k_centroid(const InstDev<T>* __restrict__ 
   const T* phi = I.phi[par];
   double s[4] = {0, 0, 0, 0};
   for (long i = (long)blockIdx.x * CT + threadIdx.x; i < n; i += (long)CB * CT) {
-    const double f = (double)phi[i];
+    const double f = (double)phi[i] + (I.phic ? (double)I.phic[i] : 0.0);  // compensated in the fused form
     const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / ((long)N * N));
     s[0] += f;
     s[1] += f * y;
@@ -58,24 +58,31 @@ __global__ void k_slice(const InstDev<T>* __restrict__ insts, int inst, int par,
   if (x >= N) return;
   const size_t NN = (size_t)N * N, plane = (size_t)zs * NN;
   const size_t o = (size_t)y * N + x;
-  const T* f[7] = {I.U[0], I.U[1], I.U[2], I.P[0], I.P[1], I.P[2], I.phi[par]};
+  // field q (vx vy vz px py pz phi) at flat index i: in the fused form the compensated value
+  auto val = [&](int q, size_t i) -> double {
+    if (q == 6) return (double)I.phi[par][i] + (I.phic ? (double)I.phic[i] : 0.0);
+    const T* f = q < 3 ? I.U[q] : I.P[q - 3];
+    double v = (double)f[i];
+    if (I.lo[q]) v += (double)__bfloat162float(I.lo[q][i]);
+    return v;
+  };
 #pragma unroll
-  for (int q = 0; q < 7; ++q) out[q * NN + o] = (double)f[q][plane + o];
+  for (int q = 0; q < 7; ++q) out[q * NN + o] = val(q, plane + o);
   // op.py: d1xO4(u) = (u[x-2] - 8u[x-1] + 8u[x+1] - u[x+2]) / (12h) along x, d1yO4 along y
   const double c = 1.0 / (12 * (double)I.ph.h);
-  auto at = [&](const T* g, int yy, int xx) {
+  auto at = [&](int q, int yy, int xx) {
     yy = (yy % N + N) % N;
     xx = (xx % N + N) % N;
-    return (double)g[plane + (size_t)yy * N + xx];
+    return val(q, plane + (size_t)yy * N + xx);
   };
-  auto dx = [&](const T* g) {
-    return c * (at(g, y, x - 2) - 8 * at(g, y, x - 1) + 8 * at(g, y, x + 1) - at(g, y, x + 2));
+  auto dx = [&](int q) {
+    return c * (at(q, y, x - 2) - 8 * at(q, y, x - 1) + 8 * at(q, y, x + 1) - at(q, y, x + 2));
   };
-  auto dy = [&](const T* g) {
-    return c * (at(g, y - 2, x) - 8 * at(g, y - 1, x) + 8 * at(g, y + 1, x) - at(g, y + 2, x));
+  auto dy = [&](int q) {
+    return c * (at(q, y - 2, x) - 8 * at(q, y - 1, x) + 8 * at(q, y + 1, x) - at(q, y + 2, x));
   };
-  out[7 * NN + o] = dx(I.U[1]) - dy(I.U[0]);  // vortex = d1xO4(vy) - d1yO4(vx)  (readDraw.py:236)
-  out[8 * NN + o] = dx(I.P[1]) - dy(I.P[0]);  // Pvortex = d1xO4(py) - d1yO4(px) (readDraw.py:237)
+  out[7 * NN + o] = dx(1) - dy(0);  // vortex = d1xO4(vy) - d1yO4(vx)  (readDraw.py:236)
+  out[8 * NN + o] = dx(4) - dy(3);  // Pvortex = d1xO4(py) - d1yO4(px) (readDraw.py:237)
 }
 
 // FP64 <-> FP32 conversion of one field on the device, for the host interface of the FP32 forms:
@@ -90,7 +97,44 @@ __global__ void k_to_f64(const float* __restrict__ src, size_t stride, double* _
     dst[i] = (double)src[i * stride] * scale;
 }
 
+// The compensated fields of the fused FP32 form: hi = the FP64 value rounded to FP32 and the
+// remainder in bf16 (lo) or, for phi, in FP32 (lo32, its update's compensation field).
+__global__ void k_split(const double* __restrict__ src, float* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
+                        float* __restrict__ lo32, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const double v = src[i];
+    const float h = __double2float_rn(v);
+    hi[i] = h;
+    const double r = v - (double)h;  // exact
+    if (lo) lo[i] = __double2bfloat16(r);
+    if (lo32) lo32[i] = __double2float_rn(r);
+  }
+}
+__global__ void k_join(const float* __restrict__ hi, const __nv_bfloat16* __restrict__ lo, const float* __restrict__ lo32,
+                       double* __restrict__ dst, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double v = (double)hi[i];
+    if (lo) v += (double)__bfloat162float(lo[i]);
+    if (lo32) v += (double)lo32[i];
+    dst[i] = v;
+  }
+}
+
+inline void check_conv(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) throw std::runtime_error(std::string(what) + " launch: " + cudaGetErrorString(e));
+}
+
 }  // namespace
+
+void launch_split(const double* src, float* hi, __nv_bfloat16* lo, float* lo32, size_t n, cudaStream_t st) {
+  k_split<<<1216, 256, 0, st>>>(src, hi, lo, lo32, n);
+  check_conv("split");
+}
+void launch_join(const float* hi, const __nv_bfloat16* lo, const float* lo32, double* dst, size_t n, cudaStream_t st) {
+  k_join<<<1216, 256, 0, st>>>(hi, lo, lo32, dst, n);
+  check_conv("join");
+}
 
 void launch_to_f32(const double* src, float* dst, size_t n, cudaStream_t st) {
   k_to_f32<<<1216, 256, 0, st>>>(src, dst, n);
