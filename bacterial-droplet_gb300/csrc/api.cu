@@ -15,6 +15,7 @@
 #include <cstring>
 #include <map>
 #include <stdexcept>
+#include <thread>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -187,6 +188,14 @@ struct ttsh_sim {
   double* post = nullptr;     // snapshot-reduction scratch (allocated on first use)
   size_t post_bytes = 0;
   int* d_err = nullptr;       // device word set by a kernel whose bounded wait ran out
+  // the asynchronous snapshot writer: one page-locked buffer (u, P, phi in FP64) that the device
+  // fills in stream order, and the host thread that formats it
+  double* conf_buf = nullptr;
+  size_t conf_cap = 0;
+  cudaEvent_t conf_ready = nullptr;
+  std::thread conf_thread;
+  int conf_rc = 0;
+  std::string conf_msg;
 
   template <class F>
   void with_engine(F&& f) {
@@ -302,10 +311,10 @@ void build_engine(ttsh_sim* s, Engine<T>& E) {
     const size_t nn = (size_t)N * N * N;
     const size_t fb = align256(nn * sizeof(T));
     // phi x2, P, u, u* x2, P* x2, the packed Poisson field W, and: fused, the phi compensation and
-    // the bf16 compensations of u, P (6) and of u*, P* x2 (12); plain, the 13 intermediates
+    // the bf16 compensations of u (3) and of u*, P* x2 (12); plain, the 13 intermediates
     const int nfields = 2 + 3 + 3 + 6 + 6 + (s->fused ? 1 : 13);
     const size_t lb = align256(nn * sizeof(__nv_bfloat16));
-    const size_t bytes = nfields * fb + align256(nn * sizeof(C)) + (s->fused ? 18 * lb : 0);
+    const size_t bytes = nfields * fb + align256(nn * sizeof(C)) + (s->fused ? 15 * lb : 0);
     char* d = nullptr;
     cudaError_t e = cudaMalloc(&d, bytes);
     if (e != cudaSuccess) throw std::bad_alloc();
@@ -332,7 +341,7 @@ void build_engine(ttsh_sim* s, Engine<T>& E) {
     if (s->fused) {
       I.phic = take();
       auto take_b = [&]() { __nv_bfloat16* p = reinterpret_cast<__nv_bfloat16*>(d + off); off += lb; return p; };
-      for (int f = 0; f < 6; ++f) I.lo[f] = take_b();
+      for (int f = 0; f < 3; ++f) I.lo[f] = take_b();
       for (int q = 0; q < 2; ++q)
         for (int f = 0; f < 6; ++f) I.slo[q][f] = take_b();
     }
@@ -422,6 +431,9 @@ void capture_graphs(ttsh_sim* s) {
 void release(ttsh_sim* s) {
   if (!s) return;
   cudaSetDevice(s->device);
+  if (s->conf_thread.joinable()) s->conf_thread.join();
+  if (s->conf_buf) cudaFreeHost(s->conf_buf);
+  if (s->conf_ready) cudaEventDestroy(s->conf_ready);
   if (s->stream) cudaStreamSynchronize(s->stream);
   for (int q = 0; q < 2; ++q)
     if (s->gexec[q]) cudaGraphExecDestroy(s->gexec[q]);
@@ -615,9 +627,9 @@ struct TrialBackup {
       if (I.phic) arrays.push_back({I.phic, n * sizeof(T)});
       arrays.push_back({I.W, 2 * n * sizeof(T)});
       if (I.wmax) arrays.push_back({I.wmax, 2 * sizeof(int)});  // the pressures' scales
-      if (I.smax) {  // the fused form's compensations of u, P and the grid of its next divergence
+      if (I.smax) {  // the fused form's compensation of u and the grid of its next divergence
         arrays.push_back({I.smax, 2 * sizeof(int)});
-        for (int f = 0; f < 6; ++f) arrays.push_back({I.lo[f], n * sizeof(__nv_bfloat16)});
+        for (int f = 0; f < 3; ++f) arrays.push_back({I.lo[f], n * sizeof(__nv_bfloat16)});
       }
     }
     size_t tot = 0;
@@ -807,7 +819,7 @@ static double* conv_scratch(const ttsh_sim* s, const I_& I) {
 
 // The state arrays of a checkpoint, in file order, as (device pointer, bytes) of the current
 // parity: phi, P, u, u*, P* of the element type, and in the fused form then the phi compensation
-// and the bf16 compensations of u, P and of u*, P* (everything the next step reads).
+// and the bf16 compensations of u and of u*, P* (everything the next step reads).
 template <class E>
 static std::vector<std::pair<void*, size_t>> state_arrays(ttsh_sim* s, E& eng, int inst) {
   auto& I = eng.h[inst];
@@ -820,7 +832,7 @@ static std::vector<std::pair<void*, size_t>> state_arrays(ttsh_sim* s, E& eng, i
   for (int b = 0; b < 3; ++b) a.push_back({I.Ps[s->par][b], n * es});
   if (I.phic) {
     a.push_back({I.phic, n * es});
-    for (int f = 0; f < 6; ++f) a.push_back({I.lo[f], n * eb});
+    for (int f = 0; f < 3; ++f) a.push_back({I.lo[f], n * eb});
     for (int f = 0; f < 6; ++f) a.push_back({I.slo[s->par][f], n * eb});
   }
   return a;
@@ -975,7 +987,7 @@ int ttsh_set_state(ttsh_sim* s, int inst, const double* phi, const double* P, co
       put(phi, I.phi[s->par], nullptr, I.phic);
       for (int b = 0; b < 3; ++b) {
         put(u + b * n, I.U[b], I.lo[b], nullptr);
-        put(P + b * n, I.P[b], I.lo[3 + b], nullptr);
+        put(P + b * n, I.P[b], nullptr, nullptr);
         if (ustar) put(ustar + b * n, I.Us[s->par][b], I.slo[s->par][b], nullptr);
         else {
           CK(cudaMemsetAsync(I.Us[s->par][b], 0, n * sizeof(float), s->stream));
@@ -1054,7 +1066,7 @@ int ttsh_get_state(ttsh_sim* s, int inst, double* phi, double* P, double* u, dou
           };
           if (phi) get(phi, I.phi[s->par], nullptr, I.phic);
           for (int b = 0; b < 3; ++b) {
-            if (P) get(P + b * n, I.P[b], I.lo[3 + b], nullptr);
+            if (P) get(P + b * n, I.P[b], nullptr, nullptr);
             if (u) get(u + b * n, I.U[b], I.lo[b], nullptr);
           }
         }
@@ -1227,15 +1239,92 @@ int ttsh_stats_from_partials(const ttsh_sim* s, const double* partials, ttsh_sta
   return bad_any ? set_error(TTSH_E_UNSTABLE, "non-finite values in the state") : TTSH_OK;
 }
 
-int ttsh_write_conf(ttsh_sim* s, int inst, const char* path) {
+// Waits for the snapshot the writer thread is formatting; its status (and message) becomes the
+// caller's.
+static int conf_join(ttsh_sim* s) {
+  if (!s->conf_thread.joinable()) return TTSH_OK;
+  s->conf_thread.join();
+  const int rc = s->conf_rc;
+  s->conf_rc = 0;
+  return rc ? set_error(rc, s->conf_msg) : TTSH_OK;
+}
+
+int ttsh_write_conf_async(ttsh_sim* s, int inst, const char* path) {
   int rc = check_inst(s, inst);
   if (rc) return rc;
-  const int N = s->inst[inst].N;
-  const size_t n = (size_t)N * N * N;
-  std::vector<double> phi(n), P(3 * n), u(3 * n);
-  rc = ttsh_get_state(s, inst, phi.data(), P.data(), u.data(), nullptr, nullptr);
+  if (!path) return set_error(TTSH_E_INVALID, "null path");
+  rc = conf_join(s);  // one buffer: the previous snapshot is finished first
   if (rc) return rc;
-  return ttsh_format_conf(N, s->inst[inst].in.ExpoData, phi.data(), P.data(), u.data(), path);
+  return guarded([&]() -> int {
+    CK(cudaSetDevice(s->device));
+    const int N = s->inst[inst].N;
+    const size_t n = (size_t)N * N * N;
+    if (s->conf_cap < 7 * n) {
+      CK(cudaStreamSynchronize(s->stream));
+      if (s->conf_buf) CK(cudaFreeHost(s->conf_buf));
+      s->conf_buf = nullptr;
+      s->conf_cap = 0;
+      CK(cudaHostAlloc(&s->conf_buf, 7 * n * sizeof(double), cudaHostAllocDefault));
+      s->conf_cap = 7 * n;
+    }
+    if (!s->conf_ready) CK(cudaEventCreateWithFlags(&s->conf_ready, cudaEventDisableTiming));
+    double* u = s->conf_buf;
+    double* P = u + 3 * n;
+    double* phi = P + 3 * n;
+    // the device writes the FP64 values straight into the page-locked buffer (it is mapped in the
+    // unified address space), in stream order: later steps may be enqueued right away
+    s->with_engine([&](auto& E) {
+      auto& I = E.h[inst];
+      typedef typename std::decay<decltype(*I.phi[0])>::type TT;
+      if constexpr (std::is_same<TT, float>::value) {
+        if (s->fused) {
+          launch_join(I.phi[s->par], nullptr, I.phic, phi, n, s->stream);
+          for (int b = 0; b < 3; ++b) {
+            launch_join(I.U[b], I.lo[b], nullptr, u + b * n, n, s->stream);
+            launch_join(I.P[b], nullptr, nullptr, P + b * n, n, s->stream);
+          }
+        } else {
+          launch_to_f64(I.phi[s->par], 1, phi, n, 1.0, s->stream);
+          for (int b = 0; b < 3; ++b) {
+            launch_to_f64(I.U[b], 1, u + b * n, n, 1.0, s->stream);
+            launch_to_f64(I.P[b], 1, P + b * n, n, 1.0, s->stream);
+          }
+        }
+      } else {
+        CK(cudaMemcpyAsync(phi, I.phi[s->par], n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        for (int b = 0; b < 3; ++b) {
+          CK(cudaMemcpyAsync(u + b * n, I.U[b], n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+          CK(cudaMemcpyAsync(P + b * n, I.P[b], n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        }
+      }
+    });
+    CK(cudaEventRecord(s->conf_ready, s->stream));
+    const int expo = s->inst[inst].in.ExpoData, dev = s->device;
+    const std::string file = path;
+    cudaEvent_t ev = s->conf_ready;
+    s->conf_thread = std::thread([s, N, expo, dev, file, ev, u, P, phi]() {
+      cudaSetDevice(dev);
+      const cudaError_t e = cudaEventSynchronize(ev);
+      if (e != cudaSuccess) {
+        s->conf_rc = TTSH_E_CUDA;
+        s->conf_msg = std::string("snapshot copy: ") + cudaGetErrorString(e);
+        return;
+      }
+      s->conf_rc = ttsh_format_conf(N, expo, phi, P, u, file.c_str());
+      if (s->conf_rc) s->conf_msg = ttsh_last_error();
+    });
+    return TTSH_OK;
+  });
+}
+
+int ttsh_conf_wait(ttsh_sim* s) {
+  if (!s) return set_error(TTSH_E_INVALID, "null handle");
+  return conf_join(s);
+}
+
+int ttsh_write_conf(ttsh_sim* s, int inst, const char* path) {
+  int rc = ttsh_write_conf_async(s, inst, path);
+  return rc ? rc : conf_join(s);
 }
 
 int ttsh_snapshot_slice(ttsh_sim* s, int inst, double* centroid, int* index, double* slices) {
@@ -1358,15 +1447,17 @@ int ttsh_run_dirs(const char* const* dirs, int n, const ttsh_ext* ext, uint64_t 
         if (m + 1 < k) continue;  // events only happen at the k-th step (k is the minimum distance)
         if (std::floor(run[i].T / run[i].dte) > std::floor((run[i].T - run[i].Dt) / run[i].dte)) {
           const long te = (long)std::floor(run[i].T / run[i].dte);
-          rc = ttsh_write_conf(s, i, (std::string(dirs[i]) + "/conf_" + std::to_string(te) + ".dat").c_str());
+          // formatted while the next steps run
+          rc = ttsh_write_conf_async(s, i, (std::string(dirs[i]) + "/conf_" + std::to_string(te) + ".dat").c_str());
         }
         if (run[i].T > run[i].Ts) run[i].active = false;
       }
     }
     if (rc) break;
   }
+  const int wrc = ttsh_conf_wait(s);
   ttsh_destroy(s);
-  return rc;
+  return rc ? rc : wrc;
 }
 
 static const char kCkpMagic[8] = {'T', 'T', 'S', 'H', 'C', 'K', 'P', '1'};

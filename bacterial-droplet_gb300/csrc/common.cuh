@@ -44,9 +44,9 @@ struct InstDev {
   T* phic;            // fused form: compensation of the phi update (the low part lost to rounding)
   int* wmax;          // FP32 forms: max |Re W|, max |Im W| of this step's Poisson source (float bits,
                       // non-negative floats order as ints); null in the FP64 form
-  // Fused FP32 form only (null elsewhere): u, P and the u*, P* ping-pong stored compensated, the
-  // FP32 value (U, P, Us, Ps) plus, in bf16, the part of the exact value its rounding dropped
-  __nv_bfloat16* lo[6];      // u (0..2), P (3..5)
+  // Fused FP32 form only (null elsewhere): u and the u*, P* ping-pong stored compensated, the
+  // FP32 value (U, Us, Ps) plus, in bf16, the part of the exact value its rounding dropped
+  __nv_bfloat16* lo[3];      // u
   __nv_bfloat16* slo[2][6];  // u*, P* of parity q
   int* smax;                 // max |u*|, max |P*| of this step (float bits): the divergence's grid
   T* mu0;             // plain-form intermediates

@@ -9,8 +9,9 @@
 //                 the reference's stale halo for neighbours across the periodic boundary)
 //   fused_correct u*, P*, W -> u, P   (getVNew, :505-511)
 //
-// u, P and u*, P* are stored compensated: the FP32 value, which the stencils read, and in bf16
-// the part of the exact value that FP32 rounding dropped, carried through every update (TwoSum).
+// u, u* and P* are stored compensated: the FP32 value, which the stencils read, and in bf16 the
+// part of the exact value that FP32 rounding dropped, carried through every update (TwoSum); P is
+// the FP32 value nearest the exact update.
 // The divergence that feeds the pressure is taken exactly from both (fused_div): u* is nearly
 // solenoidal, so its divergence is a small difference of large values, and 1/dt amplifies
 // whatever rounding it carries into the pressure.
@@ -312,9 +313,7 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
         if (halfA) {
           cprev[k] = phic[g];
           lprev[k][0] = I.lo[0][g];
-          lprev[k][1] = I.lo[3][g];
-          lprev[k][2] = I.lo[4][g];
-          lprev[k][3] = I.lo[5][g];
+          lprev[k][1] = lprev[k][2] = lprev[k][3] = __float2bfloat16_rn(0.f);  // P: FP32 state
         } else {
           lprev[k][0] = I.lo[1][g];
           lprev[k][1] = I.lo[2][g];
@@ -497,8 +496,9 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
             }
 #pragma unroll
           for (int k = 0; k < 2; ++k) {
-            const float xr = fmaf(4.f, t[k + 1][2].x, t[k][2].x + t[k + 2][2].x) -
-                             fmaf(4.f, t[k + 1][0].x, t[k][0].x + t[k + 2][0].x);
+            // differences first, then the weighted sum of the (small) differences
+            const float xd0 = t[k][2].x - t[k][0].x, xd1 = t[k + 1][2].x - t[k + 1][0].x, xd2 = t[k + 2][2].x - t[k + 2][0].x;
+            const float xr = fmaf(4.f, xd1, xd0 + xd2);
             const float yr = fmaf(4.f, t[k + 2][1].y - t[k][1].y,
                                   (t[k + 2][0].y - t[k][0].y) + (t[k + 2][2].y - t[k][2].y));
             const float z0c = fmaf(4.f, z[k + 1][0], z[k][0] + z[k + 2][0]);
@@ -559,8 +559,9 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
           }
 #pragma unroll
           for (int k = 0; k < 2; ++k) {
-            const float2 xr = vsub(vfma(four, xa[k + 1][1], vadd(xa[k][1], xa[k + 2][1])),
-                                   vfma(four, xa[k + 1][0], vadd(xa[k][0], xa[k + 2][0])));
+            // differences first, then the weighted sum of the (small) differences
+            const float2 xr = vfma(four, vsub(xa[k + 1][1], xa[k + 1][0]),
+                                   vadd(vsub(xa[k][1], xa[k][0]), vsub(xa[k + 2][1], xa[k + 2][0])));
             const float2 yr = vfma(four, vsub(ya[k + 2][1], ya[k][1]),
                                    vadd(vsub(ya[k + 2][0], ya[k][0]), vsub(ya[k + 2][2], ya[k][2])));
             const float2 t0 = vfma(four, za[k + 1][0], vadd(za[k][0], za[k + 2][0]));
@@ -915,11 +916,17 @@ __device__ __forceinline__ void correct_segment(const InstDev<float>& I, int par
       const size_t g = (size_t)(z0 - 2 + i) * NN + gc;
       const float* qc = slot_q(i) + qy * TX + qx;
       const float gv[3] = {gx.x, gy.x, gz.x}, gp[3] = {gx.y, gy.y, gz.y};
-      // compensated: the FP32 value and, in bf16, what its rounding dropped plus u*'s compensation
+      // u compensated: the FP32 value and, in bf16, what its rounding dropped plus u*'s
+      // compensation. P: the FP32 value nearest the exact P* - dt D p_p (its compensation is not
+      // kept: carried from step to step it would also integrate the FP32 rounding of P's update
+      // where that update is a small difference of its large terms, |P| near its equilibrium,
+      // increments that an FP32 state drops)
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
         put_comp(oU[b], I.lo[b], g, qc[b * CN], -(dt * (kd * (gv[b] * du))), sl[b]);
-        put_comp(oP[b], I.lo[3 + b], g, qc[(3 + b) * CN], -(dt * (kd * (gp[b] * dp))), sl[3 + b]);
+        float e;
+        const float v = two_sum(qc[(3 + b) * CN], -(dt * (kd * (gp[b] * dp))), e);
+        oP[b][g] = v + (e + __bfloat162float(sl[3 + b]));
       }
     }
   }

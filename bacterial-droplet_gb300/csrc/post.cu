@@ -63,7 +63,7 @@ __global__ void k_slice(const InstDev<T>* __restrict__ insts, int inst, int par,
     if (q == 6) return (double)I.phi[par][i] + (I.phic ? (double)I.phic[i] : 0.0);
     const T* f = q < 3 ? I.U[q] : I.P[q - 3];
     double v = (double)f[i];
-    if (I.lo[q]) v += (double)__bfloat162float(I.lo[q][i]);
+    if (q < 3 && I.lo[q]) v += (double)__bfloat162float(I.lo[q][i]);
     return v;
   };
 #pragma unroll

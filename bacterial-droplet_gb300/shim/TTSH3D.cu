@@ -61,6 +61,8 @@ struct Api {
   int (*set_state)(ttsh_sim*, int, const double*, const double*, const double*, const double*, const double*);
   int (*step)(ttsh_sim*, int);
   int (*write_conf)(ttsh_sim*, int, const char*);
+  int (*write_conf_async)(ttsh_sim*, int, const char*);
+  int (*conf_wait)(ttsh_sim*);
   void (*destroy)(ttsh_sim*);
   const char* (*last_error)(void);
   int (*struct_size)(int);
@@ -119,7 +121,8 @@ int main() {
   Api a;
   if (!(sym(h, "ttsh_read_input", a.read_input) && sym(h, "ttsh_default_ext", a.default_ext) &&
         sym(h, "ttsh_create", a.create) && sym(h, "ttsh_set_state", a.set_state) && sym(h, "ttsh_step", a.step) &&
-        sym(h, "ttsh_write_conf", a.write_conf) && sym(h, "ttsh_destroy", a.destroy) &&
+        sym(h, "ttsh_write_conf", a.write_conf) && sym(h, "ttsh_write_conf_async", a.write_conf_async) &&
+        sym(h, "ttsh_conf_wait", a.conf_wait) && sym(h, "ttsh_destroy", a.destroy) &&
         sym(h, "ttsh_last_error", a.last_error) && sym(h, "ttsh_struct_size", a.struct_size) &&
         sym(h, "ttsh_init_reference", a.init_reference)))
     return 1;
@@ -200,12 +203,17 @@ int main() {
       return 2;
     }
     if (te >= 0) {
-      if ((rc = a.write_conf(sim, 0, (dir + "/conf_" + to_string(te) + ".dat").c_str())) != 0) {
+      // formatted and written by the library's host thread while the next steps run
+      if ((rc = a.write_conf_async(sim, 0, (dir + "/conf_" + to_string(te) + ".dat").c_str())) != 0) {
         cout << "TTSH3D: " << a.last_error() << endl;
         return 2;
       }
       progress(T, P.T0, P.Ts, tStart);
     }
+  }
+  if ((rc = a.conf_wait(sim)) != 0) {
+    cout << "TTSH3D: " << a.last_error() << endl;
+    return 2;
   }
   a.destroy(sim);
   clock_t tEnd = clock();

@@ -110,6 +110,8 @@ def _signatures():
         "ttsh_get_provisional": ([_VP, ctypes.c_int, _D, _D], ctypes.c_int),
         "ttsh_reduce": ([_VP, ctypes.c_int, ctypes.POINTER(Stats)], ctypes.c_int),
         "ttsh_write_conf": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),
+        "ttsh_write_conf_async": ([_VP, ctypes.c_int, ctypes.c_char_p], ctypes.c_int),
+        "ttsh_conf_wait": ([_VP], ctypes.c_int),
         "ttsh_reduce_all": ([_VP, ctypes.c_int, ctypes.POINTER(Stats)], ctypes.c_int),
         "ttsh_format_conf": ([ctypes.c_int, ctypes.c_int, _D, _D, _D, ctypes.c_char_p], ctypes.c_int),
         "ttsh_destroy": ([_VP], None),
@@ -352,6 +354,13 @@ class Sim:
 
     def write_conf(self, inst: int, path: str):
         _check(lib().ttsh_write_conf(self._h, inst, path.encode()))
+
+    def write_conf_async(self, inst: int, path: str):
+        """Enqueue the snapshot file; it is formatted while later steps run (conf_wait to finish)."""
+        _check(lib().ttsh_write_conf_async(self._h, inst, path.encode()))
+
+    def conf_wait(self):
+        _check(lib().ttsh_conf_wait(self._h))
 
     SLICE_NAMES = ("vx", "vy", "vz", "px", "py", "pz", "phi", "vortex", "Pvortex")
 

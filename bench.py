@@ -51,11 +51,12 @@ UNIT = "Msite*steps/s"
 # pass are separate launches here), used for the per-kernel roofline.
 B_ALG_WORDS = 34
 KERNEL_WORDS = {
-    # the fused form stores u, P, u*, P* compensated (FP32 + a bf16 remainder: half a word each)
-    "fused_rhs": 22,        # reads phi, P, u (7), their compensations (1 + 3); writes phi', u*, P* (7)
-                            # and their compensations (1 + 3)
+    # the fused form stores u, u*, P* compensated (FP32 + a bf16 remainder: half a word each)
+    "fused_rhs": 20.5,      # reads phi, P, u (7), the compensations of phi, u (1 + 1.5); writes phi',
+                            # u*, P* (7) and their compensations (1 + 3)
     "fused_div": 11,        # reads u*, P* and their compensations (6 + 3); writes the packed source W (2)
-    "fused_correct": 20,    # reads u*, P*, compensations, the packed pressure (6 + 3 + 2); writes u, P (6 + 3)
+    "fused_correct": 18.5,  # reads u*, P*, compensations, the packed pressure (6 + 3 + 2); writes u, P and
+                            # the compensation of u (6 + 1.5)
     "stage1": 17, "stage2": 27, "div": 8, "correct": 14,  # plain form
     "fft_x_fwd": 4, "fft_y_fwd": 4, "fft_z_poisson": 4, "fft_y_inv": 4, "fft_x_inv": 4,
     "fft_xy_fwd": 4, "fft_yx_inv": 4,  # x and y of a plane in one launch: W read and written once

@@ -169,6 +169,14 @@ int ttsh_stats_from_partials(const ttsh_sim* s, const double* partials, ttsh_sta
  * one line per site, y outer, x, z inner; columns "vx vy vz px py pz phi" printed as
  * fixed with 15 decimals (ExpoData == 1) or "vx vy " (ExpoData == -1). */
 int ttsh_write_conf(ttsh_sim* s, int inst, const char* path);
+/* ttsh_write_conf_async — ExpoConf (TTSH3D.cu:899-1014) without stopping the steps: enqueues the
+ * snapshot of droplet `inst` on the handle's stream and returns. The fields are converted to FP64
+ * straight into a page-locked host buffer of the handle, in stream order, and a host thread
+ * formats and writes the file (the same bytes as ttsh_write_conf) while later steps run. One
+ * snapshot is in flight at a time: a second call first waits for the previous one. */
+int ttsh_write_conf_async(ttsh_sim* s, int inst, const char* path);
+/* Waits for the snapshot in flight, if any, and returns its status. ttsh_destroy waits too. */
+int ttsh_conf_wait(ttsh_sim* s);
 
 /* Same formatter on host arrays (no GPU): for writing conf files from any source. */
 int ttsh_format_conf(int N, int expo_data, const double* phi, const double* P, const double* u,

@@ -74,3 +74,49 @@ def test_run_dirs_with_autotuning(tmp_path, monkeypatch):
             a = np.loadtxt(os.path.join(tuned[i], f))
             b = np.loadtxt(os.path.join(plain[i], f))
             np.testing.assert_allclose(a, b, rtol=0, atol=1e-12)
+
+
+def test_run_dirs_matches_the_reference_program(tmp_path):
+    """forEach.pl's sweep (one TTSH3D.out per directory, forEach.pl:33-44, :131) against the batched
+    driver: three directories with different sizes, constants and cadences, each run by the
+    reference program itself (seeded as the shim is, TTSH_SEED) and all three by one ttsh_run_dirs
+    call with the same seeds: the same snapshot files with the same values (1e-12 absolute on
+    fields printed with 15 decimals)."""
+    import subprocess
+    import sys
+
+    import numpy as np
+    import ttsh
+    from conftest import ROOT
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import make_ref
+    ttsh.lib()
+    ref_bin = make_ref.build()
+    if ref_bin is None:
+        pytest.skip("patched reference source not present")
+    specs = [dict(Nx=16, Ny=16, Nz=16, Ts=0.011, dte=0.004, eta=-0.187),
+             dict(Nx=24, Ny=24, Nz=24, Ts=0.007, dte=0.002, eta=-0.25),
+             dict(Nx=16, Ny=16, Nz=16, Ts=0.009, dte=0.006, kappa=-0.5, dt0=0.001)]
+    seed = 500
+    ours = []
+    for i, sp in enumerate(specs):
+        d = str(tmp_path / ("sweep%d" % i) / "data_1")
+        _make(d, **sp)
+        ours.append(d)
+        ref_root = tmp_path / ("ref%d" % i)
+        _make(str(ref_root / "data_1"), **sp)
+        env = dict(os.environ, TTSH_SEED=str(seed + i))
+        r = subprocess.run([ref_bin], cwd=str(ref_root), env=env, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    ttsh.run_dirs(ours, seed=seed)
+    for i in range(len(specs)):
+        rd = str(tmp_path / ("ref%d" % i) / "data_1")
+        fr = sorted(f for f in os.listdir(rd) if f.startswith("conf_"))
+        fo = sorted(f for f in os.listdir(ours[i]) if f.startswith("conf_"))
+        assert fo == fr and len(fr) >= 2, (i, fo, fr)
+        N = specs[i]["Nx"]
+        for f in fr:
+            a = np.loadtxt(os.path.join(ours[i], f))
+            b = np.loadtxt(os.path.join(rd, f))
+            assert a.shape == b.shape == (N ** 3, 7), (i, f)
+            assert np.abs(a - b).max() <= 1e-12, (i, f, np.abs(a - b).max())
