@@ -310,11 +310,12 @@ void build_engine(ttsh_sim* s, Engine<T>& E) {
     const int N = ih.N;
     const size_t nn = (size_t)N * N * N;
     const size_t fb = align256(nn * sizeof(T));
-    // phi x2, P, u, u* x2, P* x2, the packed Poisson field W, and: fused, the phi compensation and
-    // the bf16 compensations of u (3) and of u*, P* x2 (12); plain, the 13 intermediates
-    const int nfields = 2 + 3 + 3 + 6 + 6 + (s->fused ? 1 : 13);
+    // phi x2, P, u, u* x2, P* x2, the packed Poisson field W, and: fused, the phi compensation,
+    // the bf16 compensations of u (3) and the bf16 pairs compensating u*, P* x2 (6 FP32 slots);
+    // plain, the 13 intermediates
+    const int nfields = 2 + 3 + 3 + 6 + 6 + (s->fused ? 1 + 6 : 13);
     const size_t lb = align256(nn * sizeof(__nv_bfloat16));
-    const size_t bytes = nfields * fb + align256(nn * sizeof(C)) + (s->fused ? 15 * lb : 0);
+    const size_t bytes = nfields * fb + align256(nn * sizeof(C)) + (s->fused ? 3 * lb : 0);
     char* d = nullptr;
     cudaError_t e = cudaMalloc(&d, bytes);
     if (e != cudaSuccess) throw std::bad_alloc();
@@ -334,16 +335,25 @@ void build_engine(ttsh_sim* s, Engine<T>& E) {
     I.phi[0] = take(); I.phi[1] = take();
     for (int b = 0; b < 3; ++b) I.P[b] = take();
     for (int b = 0; b < 3; ++b) I.U[b] = take();
-    for (int q = 0; q < 2; ++q)
-      for (int b = 0; b < 3; ++b) I.Us[q][b] = take();
-    for (int q = 0; q < 2; ++q)
-      for (int b = 0; b < 3; ++b) I.Ps[q][b] = take();
     if (s->fused) {
+      // u*, P* as pairs (u*_b, P*_b), two FP32 slots each (the same 12 slots as Us, Ps x2), in
+      // parity order: star[q] holds 3 consecutive pair fields (they double as the FP64 scratch
+      // of the host interface, 3 FP64 fields)
+      for (int q = 0; q < 2; ++q)
+        for (int b = 0; b < 3; ++b) {
+          I.star[q][b] = reinterpret_cast<float2*>(d + off);
+          off += 2 * fb;
+        }
       I.phic = take();
       auto take_b = [&]() { __nv_bfloat16* p = reinterpret_cast<__nv_bfloat16*>(d + off); off += lb; return p; };
       for (int f = 0; f < 3; ++f) I.lo[f] = take_b();
       for (int q = 0; q < 2; ++q)
-        for (int f = 0; f < 6; ++f) I.slo[q][f] = take_b();
+        for (int b = 0; b < 3; ++b) I.starlo[q][b] = reinterpret_cast<__nv_bfloat162*>(take());
+    } else {
+      for (int q = 0; q < 2; ++q)
+        for (int b = 0; b < 3; ++b) I.Us[q][b] = take();
+      for (int q = 0; q < 2; ++q)
+        for (int b = 0; b < 3; ++b) I.Ps[q][b] = take();
     }
     if (!s->fused) {
       I.mu0 = take();
@@ -813,13 +823,19 @@ static void d2h(double* dst, const T* src, size_t n, cudaStream_t st, double* sc
 template <class I_>
 static double* conv_scratch(const ttsh_sim* s, const I_& I) {
   typedef typename std::decay<decltype(*I.phi[0])>::type TT;
-  if constexpr (std::is_same<TT, float>::value) return reinterpret_cast<double*>(I.Us[s->par ^ 1][0]);
-  else return nullptr;
+  if constexpr (std::is_same<TT, float>::value) {
+    // fused: the pairs (u*, P*) of the parity not in use (24 N^3 bytes), which the next step rewrites
+    if (I.star[0][0]) return reinterpret_cast<double*>(I.star[s->par ^ 1][0]);
+    return reinterpret_cast<double*>(I.Us[s->par ^ 1][0]);
+  } else {
+    return nullptr;
+  }
 }
 
 // The state arrays of a checkpoint, in file order, as (device pointer, bytes) of the current
-// parity: phi, P, u, u*, P* of the element type, and in the fused form then the phi compensation
-// and the bf16 compensations of u and of u*, P* (everything the next step reads).
+// parity: phi, P, u of the element type, then u*, P* (the fused form: the (u*_b, P*_b) pairs, the
+// phi compensation and the bf16 compensations of u and of the pairs): everything the next step
+// reads.
 template <class E>
 static std::vector<std::pair<void*, size_t>> state_arrays(ttsh_sim* s, E& eng, int inst) {
   auto& I = eng.h[inst];
@@ -828,13 +844,15 @@ static std::vector<std::pair<void*, size_t>> state_arrays(ttsh_sim* s, E& eng, i
   std::vector<std::pair<void*, size_t>> a = {{I.phi[s->par], n * es}};
   for (int b = 0; b < 3; ++b) a.push_back({I.P[b], n * es});
   for (int b = 0; b < 3; ++b) a.push_back({I.U[b], n * es});
-  for (int b = 0; b < 3; ++b) a.push_back({I.Us[s->par][b], n * es});
-  for (int b = 0; b < 3; ++b) a.push_back({I.Ps[s->par][b], n * es});
-  if (I.phic) {
+  if (I.phic) {  // fused: the pairs (u*_b, P*_b) and their compensations
+    for (int b = 0; b < 3; ++b) a.push_back({I.star[s->par][b], 2 * n * es});
     a.push_back({I.phic, n * es});
     for (int f = 0; f < 3; ++f) a.push_back({I.lo[f], n * eb});
-    for (int f = 0; f < 6; ++f) a.push_back({I.slo[s->par][f], n * eb});
+    for (int b = 0; b < 3; ++b) a.push_back({I.starlo[s->par][b], 2 * n * eb});
+    return a;
   }
+  for (int b = 0; b < 3; ++b) a.push_back({I.Us[s->par][b], n * es});
+  for (int b = 0; b < 3; ++b) a.push_back({I.Ps[s->par][b], n * es});
   return a;
 }
 
@@ -982,22 +1000,25 @@ int ttsh_set_state(ttsh_sim* s, int inst, const double* phi, const double* P, co
       double* scr = conv_scratch(s, I);
       auto put = [&](const double* src, float* hi, __nv_bfloat16* lo, float* lo32) {
         CK(cudaMemcpyAsync(scr, src, n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
-        launch_split(scr, hi, lo, lo32, n, s->stream);
+        launch_split(scr, hi, lo, lo32, n, 1, s->stream);
+      };
+      auto put2 = [&](const double* src, float* hi, __nv_bfloat16* lo) {  // one half of the pairs
+        CK(cudaMemcpyAsync(scr, src, n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+        launch_split(scr, hi, lo, nullptr, n, 2, s->stream);
       };
       put(phi, I.phi[s->par], nullptr, I.phic);
       for (int b = 0; b < 3; ++b) {
         put(u + b * n, I.U[b], I.lo[b], nullptr);
         put(P + b * n, I.P[b], nullptr, nullptr);
-        if (ustar) put(ustar + b * n, I.Us[s->par][b], I.slo[s->par][b], nullptr);
-        else {
-          CK(cudaMemsetAsync(I.Us[s->par][b], 0, n * sizeof(float), s->stream));
-          CK(cudaMemsetAsync(I.slo[s->par][b], 0, n * sizeof(__nv_bfloat16), s->stream));
+        // the previous u*, P* (the stale halo of the first divergence) into the pairs' halves
+        float* sh = reinterpret_cast<float*>(I.star[s->par][b]);
+        __nv_bfloat16* sl = reinterpret_cast<__nv_bfloat16*>(I.starlo[s->par][b]);
+        if (!ustar || !Pstar) {
+          CK(cudaMemsetAsync(sh, 0, 2 * n * sizeof(float), s->stream));
+          CK(cudaMemsetAsync(sl, 0, 2 * n * sizeof(__nv_bfloat16), s->stream));
         }
-        if (Pstar) put(Pstar + b * n, I.Ps[s->par][b], I.slo[s->par][3 + b], nullptr);
-        else {
-          CK(cudaMemsetAsync(I.Ps[s->par][b], 0, n * sizeof(float), s->stream));
-          CK(cudaMemsetAsync(I.slo[s->par][3 + b], 0, n * sizeof(__nv_bfloat16), s->stream));
-        }
+        if (ustar) put2(ustar + b * n, sh, sl);
+        if (Pstar) put2(Pstar + b * n, sh + 1, sl + 1);
       }
       CK(cudaMemsetAsync(I.smax, 0, 2 * sizeof(int), s->stream));
       CK(cudaStreamSynchronize(s->stream));
@@ -1061,7 +1082,7 @@ int ttsh_get_state(ttsh_sim* s, int inst, double* phi, double* P, double* u, dou
       if constexpr (std::is_same<TT, float>::value) {
         if (s->fused) {  // the compensated values
           auto get = [&](double* dst, const float* hi, const __nv_bfloat16* lo, const float* lo32) {
-            launch_join(hi, lo, lo32, scr, n, s->stream);
+            launch_join(hi, lo, lo32, scr, n, 1, s->stream);
             CK(cudaMemcpyAsync(dst, scr, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
           };
           if (phi) get(phi, I.phi[s->par], nullptr, I.phic);
@@ -1109,13 +1130,15 @@ int ttsh_get_provisional(ttsh_sim* s, int inst, double* ustar, double* Pstar) {
       double* scr = conv_scratch(s, I);
       for (int b = 0; b < 3; ++b) {
         if constexpr (std::is_same<TT, float>::value) {
-          if (s->fused) {  // the last step's u*, P*, compensated
+          if (s->fused) {  // the last step's u*, P*, compensated (the halves of the pairs)
+            const float* sh = reinterpret_cast<const float*>(I.star[s->par][b]);
+            const __nv_bfloat16* sl = reinterpret_cast<const __nv_bfloat16*>(I.starlo[s->par][b]);
             if (ustar) {
-              launch_join(I.Us[s->par][b], I.slo[s->par][b], nullptr, scr, n, s->stream);
+              launch_join(sh, sl, nullptr, scr, n, 2, s->stream);
               CK(cudaMemcpyAsync(ustar + b * n, scr, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
             }
             if (Pstar) {
-              launch_join(I.Ps[s->par][b], I.slo[s->par][3 + b], nullptr, scr, n, s->stream);
+              launch_join(sh + 1, sl + 1, nullptr, scr, n, 2, s->stream);
               CK(cudaMemcpyAsync(Pstar + b * n, scr, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
             }
             continue;
@@ -1278,10 +1301,10 @@ int ttsh_write_conf_async(ttsh_sim* s, int inst, const char* path) {
       typedef typename std::decay<decltype(*I.phi[0])>::type TT;
       if constexpr (std::is_same<TT, float>::value) {
         if (s->fused) {
-          launch_join(I.phi[s->par], nullptr, I.phic, phi, n, s->stream);
+          launch_join(I.phi[s->par], nullptr, I.phic, phi, n, 1, s->stream);
           for (int b = 0; b < 3; ++b) {
-            launch_join(I.U[b], I.lo[b], nullptr, u + b * n, n, s->stream);
-            launch_join(I.P[b], nullptr, nullptr, P + b * n, n, s->stream);
+            launch_join(I.U[b], I.lo[b], nullptr, u + b * n, n, 1, s->stream);
+            launch_join(I.P[b], nullptr, nullptr, P + b * n, n, 1, s->stream);
           }
         } else {
           launch_to_f64(I.phi[s->par], 1, phi, n, 1.0, s->stream);

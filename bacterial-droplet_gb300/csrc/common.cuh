@@ -45,10 +45,12 @@ struct InstDev {
   int* wmax;          // FP32 forms: max |Re W|, max |Im W| of this step's Poisson source (float bits,
                       // non-negative floats order as ints); null in the FP64 form
   // Fused FP32 form only (null elsewhere): u and the u*, P* ping-pong stored compensated, the
-  // FP32 value (U, Us, Ps) plus, in bf16, the part of the exact value its rounding dropped
-  __nv_bfloat16* lo[3];      // u
-  __nv_bfloat16* slo[2][6];  // u*, P* of parity q
-  int* smax;                 // max |u*|, max |P*| of this step (float bits): the divergence's grid
+  // FP32 value plus, in bf16, the part of the exact value its rounding dropped; u*, P* as pairs
+  // (u*_b, P*_b), which the divergence and the correction read together
+  __nv_bfloat16* lo[3];            // u
+  float2* star[2][3];              // (u*_b, P*_b) of parity q (Us, Ps are null in the fused form)
+  __nv_bfloat162* starlo[2][3];    // their compensations
+  int* smax;                       // max |u*|, max |P*| of this step (float bits): the divergence's grid
   T* mu0;             // plain-form intermediates
   T* mu[3];
   T* sig[9];          // sig[a*3+b] = phi * D_a P_b

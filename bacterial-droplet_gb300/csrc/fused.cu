@@ -193,11 +193,13 @@ __device__ __forceinline__ float two_sum(float a, float b, float& e) {
 
 // x* = x + d stored compensated: the FP32 sum and, in bf16, what its rounding dropped plus the
 // compensation x_lo that x brought along. Returns the FP32 value.
-__device__ __forceinline__ float put_comp(float* hi, __nv_bfloat16* lo, size_t g, float x, float d, __nv_bfloat16 x_lo) {
+// `stride` 2 for one half of the pairs star / starlo.
+__device__ __forceinline__ float put_comp(float* hi, __nv_bfloat16* lo, size_t g, float x, float d, __nv_bfloat16 x_lo,
+                                          int stride = 1) {
   float e;
   const float s = two_sum(x, d, e);
-  hi[g] = s;
-  lo[g] = __float2bfloat16_rn(e + __bfloat162float(x_lo));
+  hi[stride * g] = s;
+  lo[stride * g] = __float2bfloat16_rn(e + __bfloat162float(x_lo));
   return s;
 }
 
@@ -211,9 +213,17 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
   const float* __restrict__ gphi = I.phi[par];
   const float* __restrict__ gP[3] = {I.P[0], I.P[1], I.P[2]};
   const float* __restrict__ gU[3] = {I.U[0], I.U[1], I.U[2]};
-  float* const oUs[3] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2]};
-  float* const oPs[3] = {I.Ps[par ^ 1][0], I.Ps[par ^ 1][1], I.Ps[par ^ 1][2]};
-  __nv_bfloat16* const* oSlo = I.slo[par ^ 1];
+  // u*_b and P*_b: the two halves of the pairs star[b] (and of their compensations starlo[b])
+  float* oUs[3];
+  float* oPs[3];
+  __nv_bfloat16* oSlo[6];
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    oUs[b] = reinterpret_cast<float*>(I.star[par ^ 1][b]);
+    oPs[b] = oUs[b] + 1;
+    oSlo[b] = reinterpret_cast<__nv_bfloat16*>(I.starlo[par ^ 1][b]);
+    oSlo[3 + b] = oSlo[b] + 1;
+  }
   float amu = 0.f, amp = 0.f;  // max |u*|, |P*| of this thread's outputs (the divergence's grid)
   float* const ophi = I.phi[par ^ 1];
   float* const phic = I.phic;
@@ -520,12 +530,12 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
             const float2 A0 = ac[oa], A1 = ac[ANP + oa];
             // u*_x = u_x + dt d/dt u_x (:480-482)
             const float usx = put_comp(oUs[0], oSlo[0], g, sU01[sl * BNP + ob].x, p.dt * fmaf(sk.d, dvx[k], q0.x),
-                                       lprev[k][0]);
+                                       lprev[k][0], 2);
             // P*_b = P_b + dt (pointwise part + eta L mu_b) (:623-629, :486-488)
-            const float psx = put_comp(oPs[0], oSlo[3], g, A0.y, p.dt * fmaf(p.eta, lm[k][0].y, q2.x), lprev[k][1]);
+            const float psx = put_comp(oPs[0], oSlo[3], g, A0.y, p.dt * fmaf(p.eta, lm[k][0].y, q2.x), lprev[k][1], 2);
             const float2 dp2 = vmul(vsplat(p.dt, float2()), vfma(vsplat(p.eta, float2()), lm[k][1], f2(q2.y, q3.x)));
-            const float psy = put_comp(oPs[1], oSlo[4], g, A1.x, dp2.x, lprev[k][2]);
-            const float psz = put_comp(oPs[2], oSlo[5], g, A1.y, dp2.y, lprev[k][3]);
+            const float psy = put_comp(oPs[1], oSlo[4], g, A1.x, dp2.x, lprev[k][2], 2);
+            const float psz = put_comp(oPs[2], oSlo[5], g, A1.y, dp2.y, lprev[k][3], 2);
             amu = fmaxf(amu, fabsf(usx));
             amp = fmaxf(amp, fmaxf(fabsf(psx), fmaxf(fabsf(psy), fabsf(psz))));
             // phi' = phi + dt (-u.D phi + gamma L mu_0) (:631, :515), compensated: the part of
@@ -582,8 +592,8 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
             const float2 q0 = pq[0 * CNP + c], q1 = pq[1 * CNP + c];
             // (u*_y, u*_z) = (u_y, u_z) + dt d/dt (u_y, u_z) (:480-482)
             const float2 du = vmul(vsplat(p.dt, float2()), vfma(vsplat(sk.d, float2()), dv[k], f2(q0.y, q1.x)));
-            const float usy = put_comp(oUs[1], oSlo[1], g, sU01[sl * BNP + ob].y, du.x, lprev[k][0]);
-            const float usz = put_comp(oUs[2], oSlo[2], g, sU2[sl * BNP + ob], du.y, lprev[k][1]);
+            const float usy = put_comp(oUs[1], oSlo[1], g, sU01[sl * BNP + ob].y, du.x, lprev[k][0], 2);
+            const float usz = put_comp(oUs[2], oSlo[2], g, sU2[sl * BNP + ob], du.y, lprev[k][1], 2);
             amu = fmaxf(amu, fmaxf(fabsf(usy), fabsf(usz)));
           }
         }
@@ -631,23 +641,24 @@ __global__ void __launch_bounds__(NT, 2) k_fused_rhs(const InstDev<float>* __res
 // fused_div / fused_correct: one tile column per thread; each staged plane is read once, its
 // in-plane partial sums carried in z (as in fused_rhs phase 2), so the ring only has to cover
 // the copies in flight: DR slots, the plane read and DR - 1 planes in flight. Rows are staged in
-// 16-byte chunks: a row starts at a multiple of 4 floats (2 float2) left of the tile, so every
-// chunk, wrapped or not, is one aligned 16-byte global segment (N is a multiple of 32).
+// 16-byte chunks starting a whole chunk left of the tile, so every chunk, wrapped or not, is one
+// aligned 16-byte global segment (N is a multiple of 32).
 constexpr int NTC = TX * TY;            // 512 threads
 constexpr int SH = TY + 2;              // staged rows y0 - 1 .. y0 + TY
-constexpr int SW = TX + 8;              // fused_div row, floats x0 - 4 .. x0 + TX + 3
 constexpr int CW = TX + 4;              // fused_correct row, float2 x0 - 2 .. x0 + TX + 1
 constexpr int CPL = CW * SH;            // float2 per staged plane
 constexpr int DR = 4;                   // ring slots of fused_correct
 // fused_div: a taller tile (TX x TYD) and a 2-slot ring (1 plane in flight); each slot holds the
-// FP32 values of u*, P* and their bf16 compensations (rows x0 - 8 .. x0 + TX + 7, 16-byte chunks)
-constexpr int TYD = 32, SHD = TYD + 2, SPLD = SW * SHD, DRD = 2;
-constexpr int SWB = TX + 16, SPLB = SWB * SHD;
-constexpr size_t DIV_SLOT = 6 * SPLD * sizeof(float) + 6 * SPLB * sizeof(__nv_bfloat16);
+// pairs (u*_b, P*_b) (rows x0 - 2 .. x0 + TX + 1, 16-byte chunks of 2 sites) and their bf16
+// compensations (rows x0 - 4 .. x0 + TX + 3, chunks of 4 sites)
+constexpr int TYD = 32, SHD = TYD + 2, DRD = 2;
+constexpr int SWP = TX + 4, SPLP = SWP * SHD;  // float2 per row, per plane
+constexpr int SWL = TX + 8, SPLL = SWL * SHD;  // bf16x2 per row, per plane
+constexpr size_t DIV_SLOT = 3 * SPLP * sizeof(float2) + 3 * SPLL * sizeof(__nv_bfloat162);
 constexpr size_t DIV_SMEM = DRD * DIV_SLOT;
-static_assert((6 * SPLD * sizeof(float)) % 16 == 0 && DIV_SLOT % 16 == 0, "16-byte aligned staging");
+static_assert((3 * SPLP * sizeof(float2)) % 16 == 0 && DIV_SLOT % 16 == 0, "16-byte aligned staging");
 static_assert(2 * DIV_SMEM <= 227 * 1024, "fused_div: two CTAs per SM");
-constexpr size_t COR_SLOT = CPL * sizeof(float2) + 6 * CN * sizeof(float);  // p_v, p_p on B; u*, P* on C
+constexpr size_t COR_SLOT = CPL * sizeof(float2) + 3 * CN * sizeof(float2);  // p_v, p_p on B; (u*, P*) pairs on C
 constexpr size_t COR_SMEM = DR * COR_SLOT;
 
 // wait until at most DR - 2 copy groups are pending: the group of the plane read now is complete
@@ -680,20 +691,15 @@ __device__ __forceinline__ float split_grid(int mbits) {
 __device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, int N, int x0, int y0, int z0, int z1,
                                             unsigned char* sm) {
   const size_t NN = (size_t)N * N;
-  const float* cur[6] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2],
-                         I.Ps[par ^ 1][0], I.Ps[par ^ 1][1], I.Ps[par ^ 1][2]};
-  const float* old[6] = {I.Us[par][0], I.Us[par][1], I.Us[par][2], I.Ps[par][0], I.Ps[par][1], I.Ps[par][2]};
-  const __nv_bfloat16* const* curl = I.slo[par ^ 1];
-  const __nv_bfloat16* const* oldl = I.slo[par];
   float2* const oW = I.W;
   const int stale_q2 = I.stale;
   const float kd = I.ph.c2h * (1.f / 36.f) * I.ph.inv_dt;  // d/36 of the 27-point D, and 1/dt
   const float2 S = f2(split_grid(I.smax[0]), split_grid(I.smax[1]));
   const int tid = threadIdx.x;
   const int niter = (z1 - z0) + 2;
-  auto slot_f = [&](int i) { return reinterpret_cast<float*>(sm + (i % DRD) * DIV_SLOT); };
-  auto slot_b = [&](int i) {
-    return reinterpret_cast<__nv_bfloat16*>(sm + (i % DRD) * DIV_SLOT + 6 * SPLD * sizeof(float));
+  auto slot_p = [&](int i) { return reinterpret_cast<float2*>(sm + (i % DRD) * DIV_SLOT); };
+  auto slot_l = [&](int i) {
+    return reinterpret_cast<__nv_bfloat162*>(sm + (i % DRD) * DIV_SLOT + 3 * SPLP * sizeof(float2));
   };
   // issue(i): plane z0 - 1 + i into slot i % DRD (an empty group past the last plane, so that
   // every iteration commits one). Chunks outside the domain come from the previous step's u*, P*
@@ -703,35 +709,35 @@ __device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, in
     const int zu = z0 - 1 + i;
     const bool zw = zu < 0 || zu >= N;
     const int zz = wrapN(zu, N);
-    float* dst = slot_f(i);
-    __nv_bfloat16* dsb = slot_b(i);
-    constexpr int CR = SW / 4, CRB = SWB / 8;  // chunks per row
-    for (int t = tid; t < SHD * (CR + CRB); t += NTV) {
-      const bool lo = t >= SHD * CR;
-      const int tt = lo ? t - SHD * CR : t, cr = lo ? CRB : CR;
+    float2* dp = slot_p(i);
+    __nv_bfloat162* dl = slot_l(i);
+    constexpr int CP2 = SWP / 2, CL4 = SWL / 4;  // chunks per row
+    for (int t = tid; t < SHD * (CP2 + CL4); t += NTV) {
+      const bool lo = t >= SHD * CP2;
+      const int tt = lo ? t - SHD * CP2 : t, cr = lo ? CL4 : CP2;
       const int ry = tt / cr, rc = tt - ry * cr;
-      const int gx = lo ? x0 - 8 + 8 * rc : x0 - 4 + 4 * rc, gy = y0 - 1 + ry;
-      const bool stale = stale_q2 && (zw || gx < 0 || gx >= N || gy < 0 || gy >= N);
+      const int gx = lo ? x0 - 4 + 4 * rc : x0 - 2 + 2 * rc, gy = y0 - 1 + ry;
+      const int q = (stale_q2 && (zw || gx < 0 || gx >= N || gy < 0 || gy >= N)) ? par : par ^ 1;
       const size_t g = (size_t)zz * NN + (size_t)wrapN(gy, N) * N + wrapN(gx, N);
       if (lo) {
 #pragma unroll
-        for (int f = 0; f < 6; ++f) cp_async16(dsb + f * SPLB + ry * SWB + 8 * rc, (stale ? oldl[f] : curl[f]) + g);
+        for (int f = 0; f < 3; ++f) cp_async16(dl + f * SPLL + ry * SWL + 4 * rc, I.starlo[q][f] + g);
       } else {
 #pragma unroll
-        for (int f = 0; f < 6; ++f) cp_async16(dst + f * SPLD + ry * SW + 4 * rc, (stale ? old[f] : cur[f]) + g);
+        for (int f = 0; f < 3; ++f) cp_async16(dp + f * SPLP + ry * SWP + 2 * rc, I.star[q][f] + g);
       }
     }
     cp_async_commit();
   };
   const int qx = tid % TX, qy0 = (tid / TX) * USD;
   const size_t gc0 = (size_t)(y0 + qy0) * N + (x0 + qx);
-  const int wbase = qy0 * SW + (qx + 3);    // staged FP32 index of window row 0, column x - 1
-  const int wbaseB = qy0 * SWB + (qx + 7);  // staged bf16 index of the same
-  // column x sits at the even staged index qx + 4 (rows and planes have even lengths), so the
-  // aligned pair holding it starts at column offset pb of the window and the third column is sc
+  const int wbp = qy0 * SWP + (qx + 1);  // staged pair index of window row 0, column x - 1
+  const int wbl = qy0 * SWL + (qx + 3);  // the same in the compensation rows
+  // column x sits at the even staged indices qx + 2 (pairs) and qx + 4 (compensations), so the
+  // aligned two-column load that holds it starts at window column pb and the third column is sc
   const bool odd = (qx & 1) != 0;
   const int pb = odd ? 0 : 1, sc = odd ? 2 : 0;
-  static_assert(SW % 2 == 0 && SPLD % 2 == 0, "aligned column pairs in the staged rows");
+  static_assert(SWP % 2 == 0 && SPLP % 2 == 0 && SWL % 2 == 0 && SPLL % 2 == 0, "aligned column pairs");
   // the divergence D_x v_x + D_y v_y + D_z v_z of v = (u*, P*) (getStream mode 0, :664-670), each
   // D = d/36 delta s s: a plane adds Q = delta_x s_y v_x + s_x delta_y v_y with weight s_z =
   // (1, 4, 1) and Z = s_x s_y v_z with weight delta_z = (-1, 0, 1) over planes c-1, c, c+1.
@@ -745,54 +751,50 @@ __device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, in
   for (int k = 0; k < USD; ++k) rD1[0][k] = rD2[0][k] = rD1[1][k] = rD2[1][k] = f2(0.f, 0.f);
   float amx = 0.f, amy = 0.f;  // max |Re W|, |Im W| of this thread's outputs
   const float2 four = f2(4.f, 4.f);
+  auto split = [&](float2 hi, __nv_bfloat162 lo, float2& q, float2& rest) {
+    q = vsub(vadd(hi, S), S);
+    rest = vadd(vsub(hi, q), __bfloat1622float2(lo));
+  };
 #pragma unroll
   for (int k = 0; k < DRD - 1; ++k) issue(k);
   for (int i = 0; i < niter; ++i) {
     cp_async_wait_div();
     __syncthreads();
     issue(i + DRD - 1);  // into the slot read at iteration i - 1
-    const float* s = slot_f(i) + wbase;
-    const __nv_bfloat16* sb = slot_b(i) + wbaseB;
-    // value (u*, P*) of component comp at window row r, column c, split into (q, s)
-    auto split = [&](float2 hi, float2 lo, float2& q, float2& rest) {
-      q = vsub(vadd(hi, S), S);
-      rest = vadd(vsub(hi, q), lo);
-    };
-    auto lo2 = [&](int comp, int r, int c) {
-      return f2(__bfloat162float(sb[comp * SPLB + r * SWB + c]), __bfloat162float(sb[(3 + comp) * SPLB + r * SWB + c]));
-    };
-    // the three columns x - 1, x, x + 1 of field f in window row r with two loads: the aligned
-    // pair that holds x (x - 1, x for odd x; x, x + 1 for even x) and the remaining column
-    auto row3 = [&](int f, int r, float& c0, float& c1, float& c2) {
-      const float* q = s + f * SPLD + r * SW;
-      const float2 pr = *reinterpret_cast<const float2*>(q + pb);
-      const float sv = q[sc];
-      c0 = odd ? pr.x : sv;
-      c1 = odd ? pr.y : pr.x;
-      c2 = odd ? sv : pr.y;
+    const float2* sp = slot_p(i) + wbp;
+    const __nv_bfloat162* sl = slot_l(i) + wbl;
+    // the three columns x - 1, x, x + 1 of component f in window row r, split: the aligned
+    // two-column loads that hold x and the remaining column
+    auto row3 = [&](int f, int r, float2* q, float2* rest) {
+      const float2* a = sp + f * SPLP + r * SWP;
+      const __nv_bfloat162* b = sl + f * SPLL + r * SWL;
+      const float4 pr = *reinterpret_cast<const float4*>(a + pb);
+      const float2 sv = a[sc];
+      const uint2 lr = *reinterpret_cast<const uint2*>(b + pb);
+      const __nv_bfloat162 lv = b[sc];
+      const float2 p0 = f2(pr.x, pr.y), p1 = f2(pr.z, pr.w);
+      const __nv_bfloat162 l0 = *reinterpret_cast<const __nv_bfloat162*>(&lr.x);
+      const __nv_bfloat162 l1 = *reinterpret_cast<const __nv_bfloat162*>(&lr.y);
+      split(odd ? p0 : sv, odd ? l0 : lv, q[0], rest[0]);
+      split(odd ? p1 : p0, odd ? l1 : l0, q[1], rest[1]);
+      split(odd ? sv : p1, odd ? lv : l1, q[2], rest[2]);
     };
     // per row of the window and part: the x-part delta_x v_x, and s_x of v_y and of v_z
     float2 xd[2][USD + 2], ys[2][USD + 2], zs[2][USD + 2];
 #pragma unroll
     for (int r = 0; r < USD + 2; ++r) {
       float2 q0, s0, q2, s2;
-      split(f2(s[r * SW], s[3 * SPLD + r * SW]), lo2(0, r, 0), q0, s0);
-      split(f2(s[r * SW + 2], s[3 * SPLD + r * SW + 2]), lo2(0, r, 2), q2, s2);
+      split(sp[r * SWP], sl[r * SWL], q0, s0);
+      split(sp[r * SWP + 2], sl[r * SWL + 2], q2, s2);
       xd[0][r] = vsub(q2, q0);
       xd[1][r] = vsub(s2, s0);
-#pragma unroll
-      for (int comp = 1; comp <= 2; ++comp) {
-        float a[3], b[3];
-        row3(comp, r, a[0], a[1], a[2]);
-        row3(3 + comp, r, b[0], b[1], b[2]);
-        float2 qc[3], sc3[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) split(f2(a[c], b[c]), lo2(comp, r, c), qc[c], sc3[c]);
-        const float2 vq = vfma(four, qc[1], vadd(qc[0], qc[2]));
-        const float2 vs = vfma(four, sc3[1], vadd(sc3[0], sc3[2]));
-        if (comp == 1) { ys[0][r] = vq; ys[1][r] = vs; }
-        else { zs[0][r] = vq; zs[1][r] = vs; }
-      }
+      float2 qc[3], rc[3];
+      row3(1, r, qc, rc);
+      ys[0][r] = vfma(four, qc[1], vadd(qc[0], qc[2]));
+      ys[1][r] = vfma(four, rc[1], vadd(rc[0], rc[2]));
+      row3(2, r, qc, rc);
+      zs[0][r] = vfma(four, qc[1], vadd(qc[0], qc[2]));
+      zs[1][r] = vfma(four, rc[1], vadd(rc[0], rc[2]));
     }
 #pragma unroll
     for (int k = 0; k < USD; ++k) {
@@ -836,14 +838,12 @@ __device__ __forceinline__ void correct_segment(const InstDev<float>& I, int par
   const float du = pow2_denorm(I.wmax[0]), dp = pow2_denorm(I.wmax[1]);
   const size_t NN = (size_t)N * N;
   const int niter = (z1 - z0) + 2;
-  const float* qs[6] = {I.Us[par ^ 1][0], I.Us[par ^ 1][1], I.Us[par ^ 1][2],
-                        I.Ps[par ^ 1][0], I.Ps[par ^ 1][1], I.Ps[par ^ 1][2]};
   float* const oU[3] = {I.U[0], I.U[1], I.U[2]};
   float* const oP[3] = {I.P[0], I.P[1], I.P[2]};
   const float2* __restrict__ gW = I.W;
   const int tid = threadIdx.x;
   auto slot_w = [&](int i) { return reinterpret_cast<float2*>(smc + (i % DR) * COR_SLOT); };
-  auto slot_q = [&](int i) { return reinterpret_cast<float*>(smc + (i % DR) * COR_SLOT + CPL * sizeof(float2)); };
+  auto slot_q = [&](int i) { return reinterpret_cast<float2*>(smc + (i % DR) * COR_SLOT + CPL * sizeof(float2)); };
   // issue(i): into slot i % DR the pressures (p_v, p_p) of plane z0 - 1 + i over tile+1 and u*, P*
   // of plane z0 - 2 + i (finished at iteration i) over the tile; an empty group past the last plane
   auto issue = [&](int i) {
@@ -858,16 +858,14 @@ __device__ __forceinline__ void correct_segment(const InstDev<float>& I, int par
     }
     const int zq = z0 - 2 + i;
     if (zq >= z0) {
-      float* dq = slot_q(i);
-      // 4 groups of TY * TX / 4 threads, one chunk of a tile row each: group k copies fields k, k + 4
-      constexpr int QR = TX / 4, QG = TY * QR;  // chunks per tile row, per field
-      static_assert(4 * QG == NTC, "chunk groups cover the block");
-      const int r = tid % QG, fg = tid / QG;
-      const int ry = r / QR, rc = r - ry * QR;
-      const size_t go = (size_t)zq * NN + (size_t)(y0 + ry) * N + x0 + 4 * rc;
-#pragma unroll
-      for (int f = 0; f < 6; ++f)
-        if ((f & 3) == fg) cp_async16(dq + f * CN + ry * TX + 4 * rc, qs[f] + go);
+      // the pairs (u*_b, P*_b) over the tile: 16-byte chunks of 2 sites
+      float2* dq = slot_q(i);
+      constexpr int QR = TX / 2, QF = TY * QR;  // chunks per tile row, per pair field
+      for (int t = tid; t < 3 * QF; t += NTC) {
+        const int f = t / QF, r = t - f * QF;
+        const int ry = r / QR, rc = r - ry * QR;
+        cp_async16(dq + f * CN + ry * TX + 2 * rc, I.star[par ^ 1][f] + (size_t)zq * NN + (size_t)(y0 + ry) * N + x0 + 2 * rc);
+      }
     }
     cp_async_commit();
   };
@@ -879,12 +877,12 @@ __device__ __forceinline__ void correct_segment(const InstDev<float>& I, int par
 #pragma unroll
   for (int k = 0; k < DR - 1; ++k) issue(k);
   for (int i = 0; i < niter; ++i) {
-    // the compensations of u*, P* at this iteration's output site, loaded before the wait
-    __nv_bfloat16 sl[6];
+    // the compensations of (u*_b, P*_b) at this iteration's output site, loaded before the wait
+    __nv_bfloat162 sl[3];
     if (i >= 2) {
       const size_t g = (size_t)(z0 - 2 + i) * NN + gc;
 #pragma unroll
-      for (int f = 0; f < 6; ++f) sl[f] = I.slo[par ^ 1][f][g];
+      for (int f = 0; f < 3; ++f) sl[f] = I.starlo[par ^ 1][f][g];
     }
     cp_async_wait_ring();
     __syncthreads();
@@ -914,7 +912,7 @@ __device__ __forceinline__ void correct_segment(const InstDev<float>& I, int par
     if (i >= 2) {
       // getVNew (TTSH3D.cu:505-511): u = u* - dt D p_v, P = P* - dt D p_p
       const size_t g = (size_t)(z0 - 2 + i) * NN + gc;
-      const float* qc = slot_q(i) + qy * TX + qx;
+      const float2* qc = slot_q(i) + qy * TX + qx;
       const float gv[3] = {gx.x, gy.x, gz.x}, gp[3] = {gx.y, gy.y, gz.y};
       // u compensated: the FP32 value and, in bf16, what its rounding dropped plus u*'s
       // compensation. P: the FP32 value nearest the exact P* - dt D p_p (its compensation is not
@@ -923,10 +921,11 @@ __device__ __forceinline__ void correct_segment(const InstDev<float>& I, int par
       // increments that an FP32 state drops)
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
-        put_comp(oU[b], I.lo[b], g, qc[b * CN], -(dt * (kd * (gv[b] * du))), sl[b]);
+        const float2 st = qc[b * CN];
+        put_comp(oU[b], I.lo[b], g, st.x, -(dt * (kd * (gv[b] * du))), __low2bfloat16(sl[b]));
         float e;
-        const float v = two_sum(qc[(3 + b) * CN], -(dt * (kd * (gp[b] * dp))), e);
-        oP[b][g] = v + (e + __bfloat162float(sl[3 + b]));
+        const float v = two_sum(st.y, -(dt * (kd * (gp[b] * dp))), e);
+        oP[b][g] = v + (e + __bfloat162float(__high2bfloat16(sl[b])));
       }
     }
   }

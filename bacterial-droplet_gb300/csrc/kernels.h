@@ -77,9 +77,11 @@ void fused_prepare();
 void launch_to_f32(const double* src, float* dst, size_t n, cudaStream_t st);
 void launch_to_f64(const float* src, size_t stride, double* dst, size_t n, double scale, cudaStream_t st);
 // The fused FP32 form's compensated fields (post.cu): an FP64 field split into its FP32 value and
-// the remainder (bf16 lo or FP32 lo32), and joined back.
-void launch_split(const double* src, float* hi, __nv_bfloat16* lo, float* lo32, size_t n, cudaStream_t st);
-void launch_join(const float* hi, const __nv_bfloat16* lo, const float* lo32, double* dst, size_t n, cudaStream_t st);
+// the remainder (bf16 lo or FP32 lo32), and joined back; hi and lo strided (2: one half of a pair
+// field).
+void launch_split(const double* src, float* hi, __nv_bfloat16* lo, float* lo32, size_t n, int stride, cudaStream_t st);
+void launch_join(const float* hi, const __nv_bfloat16* lo, const float* lo32, double* dst, size_t n, int stride,
+                 cudaStream_t st);
 int centroid_blocks();
 template <class T> void launch_centroid(const InstDev<T>* d_all, int inst, int par, double* part, cudaStream_t st);
 template <class T>

@@ -99,22 +99,23 @@ __global__ void k_to_f64(const float* __restrict__ src, size_t stride, double* _
 
 // The compensated fields of the fused FP32 form: hi = the FP64 value rounded to FP32 and the
 // remainder in bf16 (lo) or, for phi, in FP32 (lo32, its update's compensation field).
+// hi and lo are read / written with `stride` (2: one half of an interleaved pair field).
 __global__ void k_split(const double* __restrict__ src, float* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
-                        float* __restrict__ lo32, size_t n) {
+                        float* __restrict__ lo32, size_t n, int stride) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const double v = src[i];
     const float h = __double2float_rn(v);
-    hi[i] = h;
+    hi[stride * i] = h;
     const double r = v - (double)h;  // exact
-    if (lo) lo[i] = __double2bfloat16(r);
+    if (lo) lo[stride * i] = __double2bfloat16(r);
     if (lo32) lo32[i] = __double2float_rn(r);
   }
 }
 __global__ void k_join(const float* __restrict__ hi, const __nv_bfloat16* __restrict__ lo, const float* __restrict__ lo32,
-                       double* __restrict__ dst, size_t n) {
+                       double* __restrict__ dst, size_t n, int stride) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    double v = (double)hi[i];
-    if (lo) v += (double)__bfloat162float(lo[i]);
+    double v = (double)hi[stride * i];
+    if (lo) v += (double)__bfloat162float(lo[stride * i]);
     if (lo32) v += (double)lo32[i];
     dst[i] = v;
   }
@@ -127,12 +128,13 @@ inline void check_conv(const char* what) {
 
 }  // namespace
 
-void launch_split(const double* src, float* hi, __nv_bfloat16* lo, float* lo32, size_t n, cudaStream_t st) {
-  k_split<<<1216, 256, 0, st>>>(src, hi, lo, lo32, n);
+void launch_split(const double* src, float* hi, __nv_bfloat16* lo, float* lo32, size_t n, int stride, cudaStream_t st) {
+  k_split<<<1216, 256, 0, st>>>(src, hi, lo, lo32, n, stride);
   check_conv("split");
 }
-void launch_join(const float* hi, const __nv_bfloat16* lo, const float* lo32, double* dst, size_t n, cudaStream_t st) {
-  k_join<<<1216, 256, 0, st>>>(hi, lo, lo32, dst, n);
+void launch_join(const float* hi, const __nv_bfloat16* lo, const float* lo32, double* dst, size_t n, int stride,
+                 cudaStream_t st) {
+  k_join<<<1216, 256, 0, st>>>(hi, lo, lo32, dst, n, stride);
   check_conv("join");
 }
 
