@@ -733,8 +733,9 @@ __device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, in
   const size_t gc0 = (size_t)(y0 + qy0) * N + (x0 + qx);
   const int wbp = qy0 * SWP + (qx + 1);  // staged pair index of window row 0, column x - 1
   const int wbl = qy0 * SWL + (qx + 3);  // the same in the compensation rows
-  // column x sits at the even staged indices qx + 2 (pairs) and qx + 4 (compensations), so the
-  // aligned two-column load that holds it starts at window column pb and the third column is sc
+  // column x sits at staged index qx + 2 (pairs) and qx + 4 (compensations), both even when qx is:
+  // the aligned two-column load that holds it starts at window column pb (1 for even qx, else 0)
+  // and the third column of the window is sc
   const bool odd = (qx & 1) != 0;
   const int pb = odd ? 0 : 1, sc = odd ? 2 : 0;
   static_assert(SWP % 2 == 0 && SPLP % 2 == 0 && SWL % 2 == 0 && SPLL % 2 == 0, "aligned column pairs");
