@@ -50,14 +50,13 @@ def test_fused_matches_plain_fp32(N, k2_mode, quirks, zeta):
 
 
 def test_fused_fp32_vs_oracle_droplet(oracle_mod):
-    """64^3 droplet, zeta = 0.01, 200 steps: FP32 fused vs FP64 oracle, 1e-5 on phi and P, 1e-3 on u, p."""
+    """64^3 droplet, zeta = 0.01, 200 steps: FP32 fused vs the FP64 oracle, every field within 1e-5."""
     import ttsh
     st = droplet_state(64)
     f = run(st, 200, ttsh.FORM_FUSED, zeta=0.01)
     o = run_oracle(oracle_mod, st, 200, 0, 1, 0.01)
     errs = field_errors(f, o)
-    assert errs["phi"] <= 1e-5 and errs["P"] <= 1e-5, errs
-    assert errs["u"] <= 1e-3 and errs["pv"] <= 1e-3 and errs["pp"] <= 1e-3, errs
+    assert max(errs.values()) <= 1e-5, errs
 
 
 def test_fused_batch_mixed_sizes_match_single():
