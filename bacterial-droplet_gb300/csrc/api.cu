@@ -792,30 +792,56 @@ void append_cache(const char* path, const std::string& key, const ttsh_tuning& t
 
 }  // namespace
 
+// Whether kernels may read and write the host range [p, p + bytes) in place: it is page-locked
+// (cudaHostAlloc / cudaHostRegister; in the unified address space its host address is also its
+// device address), checked at both ends. Pageable arrays are staged by the copy engines.
+static bool host_direct(ttsh_sim* s, const void* p, size_t bytes) {
+  (void)s;
+  if (!p || !bytes) return false;
+  const char* c = static_cast<const char*>(p);
+  for (const char* q : {c, c + bytes - 1}) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, q) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return false;
+    }
+    if (at.type != cudaMemoryTypeHost || at.devicePointer != static_cast<const void*>(q)) return false;
+  }
+  return true;
+}
+
 // Host (FP64) <-> device (T) copies of one N^3 field, asynchronous on `st` (the caller
-// synchronises). For FP32 fields the FP64 data crosses the bus as it is and is converted on the
-// device through `scratch`: n doubles of device memory that no step reads (the other half of the
-// u* ping-pong pair, which the next step overwrites before reading). Successive calls reuse it
-// in stream order.
+// synchronises). FP64 fields go through the copy engines. FP32 fields are converted on the device
+// by kernels that read (write) the host array in place when host_direct allows it, and otherwise
+// through `scratch`: n doubles of device memory that no step reads (the other half of the u*
+// ping-pong pair, which the next step overwrites before reading); successive calls reuse it in
+// stream order. scale_bits (FP32 only): see launch_to_f64.
 template <class T>
-static void h2d(T* dst, const double* src, size_t n, cudaStream_t st, double* scratch) {
+static void h2d(ttsh_sim* s, T* dst, const double* src, size_t n, double* scratch) {
+  const cudaStream_t st = s->stream;
   if constexpr (sizeof(T) == sizeof(double)) {
     CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, st));
   } else {
-    CK(cudaMemcpyAsync(scratch, src, n * sizeof(double), cudaMemcpyHostToDevice, st));
-    launch_to_f32(scratch, dst, n, st);
+    if (!host_direct(s, src, n * sizeof(double))) {
+      CK(cudaMemcpyAsync(scratch, src, n * sizeof(double), cudaMemcpyHostToDevice, st));
+      src = scratch;
+    }
+    launch_to_f32(src, dst, n, st);
   }
 }
 template <class T>
-static void d2h(double* dst, const T* src, size_t n, cudaStream_t st, double* scratch, size_t stride = 1,
-                double scale = 1.0) {
+static void d2h(ttsh_sim* s, double* dst, const T* src, size_t n, double* scratch, size_t stride = 1,
+                const int* scale_bits = nullptr) {
+  const cudaStream_t st = s->stream;
+  const bool direct = host_direct(s, dst, n * sizeof(double));
   if constexpr (sizeof(T) == sizeof(double)) {
     if (stride == 1) CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    else if (direct) launch_gather_f64(src, stride, dst, n, st);
     else CK(cudaMemcpy2DAsync(dst, sizeof(double), src, stride * sizeof(double), sizeof(double), n,
                               cudaMemcpyDeviceToHost, st));
   } else {
-    launch_to_f64(src, stride, scratch, n, scale, st);
-    CK(cudaMemcpyAsync(dst, scratch, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    launch_to_f64(src, stride, direct ? dst : scratch, n, scale_bits, st);
+    if (!direct) CK(cudaMemcpyAsync(dst, scratch, n * sizeof(double), cudaMemcpyDeviceToHost, st));
   }
 }
 // The conversion scratch of an instance: its u* buffer of the parity not in use (three
@@ -998,13 +1024,17 @@ int ttsh_set_state(ttsh_sim* s, int inst, const double* phi, const double* P, co
       // compensated fields: FP32 value + remainder; no grid for the first divergence yet
       InstDev<float>& I = s->ef.h[inst];
       double* scr = conv_scratch(s, I);
-      auto put = [&](const double* src, float* hi, __nv_bfloat16* lo, float* lo32) {
+      // the split kernel reads the host array in place when it can (host_direct), else a staged copy
+      auto stage = [&](const double* src) -> const double* {
+        if (host_direct(s, src, n * sizeof(double))) return src;
         CK(cudaMemcpyAsync(scr, src, n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
-        launch_split(scr, hi, lo, lo32, n, 1, s->stream);
+        return scr;
+      };
+      auto put = [&](const double* src, float* hi, __nv_bfloat16* lo, float* lo32) {
+        launch_split(stage(src), hi, lo, lo32, n, 1, s->stream);
       };
       auto put2 = [&](const double* src, float* hi, __nv_bfloat16* lo) {  // one half of the pairs
-        CK(cudaMemcpyAsync(scr, src, n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
-        launch_split(scr, hi, lo, nullptr, n, 2, s->stream);
+        launch_split(stage(src), hi, lo, nullptr, n, 2, s->stream);
       };
       put(phi, I.phi[s->par], nullptr, I.phic);
       for (int b = 0; b < 3; ++b) {
@@ -1028,14 +1058,14 @@ int ttsh_set_state(ttsh_sim* s, int inst, const double* phi, const double* P, co
       auto& I = E.h[inst];
       typedef typename std::decay<decltype(*I.phi[0])>::type TT;
       double* scr = conv_scratch(s, I);
-      h2d<TT>(I.phi[s->par], phi, n, s->stream, scr);
+      h2d<TT>(s, I.phi[s->par], phi, n, scr);
       if (I.phic) CK(cudaMemsetAsync(I.phic, 0, n * sizeof(TT), s->stream));
       for (int b = 0; b < 3; ++b) {
-        h2d<TT>(I.P[b], P + b * n, n, s->stream, scr);
-        h2d<TT>(I.U[b], u + b * n, n, s->stream, scr);
-        if (ustar) h2d<TT>(I.Us[s->par][b], ustar + b * n, n, s->stream, scr);
+        h2d<TT>(s, I.P[b], P + b * n, n, scr);
+        h2d<TT>(s, I.U[b], u + b * n, n, scr);
+        if (ustar) h2d<TT>(s, I.Us[s->par][b], ustar + b * n, n, scr);
         else CK(cudaMemsetAsync(I.Us[s->par][b], 0, n * sizeof(TT), s->stream));
-        if (Pstar) h2d<TT>(I.Ps[s->par][b], Pstar + b * n, n, s->stream, scr);
+        if (Pstar) h2d<TT>(s, I.Ps[s->par][b], Pstar + b * n, n, scr);
         else CK(cudaMemsetAsync(I.Ps[s->par][b], 0, n * sizeof(TT), s->stream));
       }
       CK(cudaStreamSynchronize(s->stream));
@@ -1082,6 +1112,10 @@ int ttsh_get_state(ttsh_sim* s, int inst, double* phi, double* P, double* u, dou
       if constexpr (std::is_same<TT, float>::value) {
         if (s->fused) {  // the compensated values
           auto get = [&](double* dst, const float* hi, const __nv_bfloat16* lo, const float* lo32) {
+            if (host_direct(s, dst, n * sizeof(double))) {  // joined straight into the host array
+              launch_join(hi, lo, lo32, dst, n, 1, s->stream);
+              return;
+            }
             launch_join(hi, lo, lo32, scr, n, 1, s->stream);
             CK(cudaMemcpyAsync(dst, scr, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
           };
@@ -1093,23 +1127,18 @@ int ttsh_get_state(ttsh_sim* s, int inst, double* phi, double* P, double* u, dou
         }
       }
       if (!s->fused) {
-        if (phi) d2h<TT>(phi, I.phi[s->par], n, s->stream, scr);
+        if (phi) d2h<TT>(s, phi, I.phi[s->par], n, scr);
         for (int b = 0; b < 3; ++b) {
-          if (P) d2h<TT>(P + b * n, I.P[b], n, s->stream, scr);
-          if (u) d2h<TT>(u + b * n, I.U[b], n, s->stream, scr);
+          if (P) d2h<TT>(s, P + b * n, I.P[b], n, scr);
+          if (u) d2h<TT>(s, u + b * n, I.U[b], n, scr);
         }
       }
+      // FP32: the pressures come out of the FFT scaled by powers of two (pow2_norm, common.cuh),
+      // recorded as the maxima wmax[0], wmax[1]; FP64: unscaled (wmax is null)
       const TT* w = reinterpret_cast<const TT*>(I.W);
-      double sv = 1.0, sp = 1.0;  // FP32: the pressures' power-of-two scales (pow2_norm, common.cuh)
-      if (I.wmax && (p_v || p_p)) {
-        int wm[2];
-        CK(cudaMemcpyAsync(wm, I.wmax, sizeof wm, cudaMemcpyDeviceToHost, s->stream));
-        CK(cudaStreamSynchronize(s->stream));
-        sv = pow2_denorm(wm[0]);
-        sp = pow2_denorm(wm[1]);
-      }
-      if (p_v) d2h<TT>(p_v, w, n, s->stream, scr, 2, sv);
-      if (p_p) d2h<TT>(p_p, w + 1, n, s->stream, scr, 2, sp);
+      const int* wm = I.wmax;
+      if (p_v) d2h<TT>(s, p_v, w, n, scr, 2, wm);
+      if (p_p) d2h<TT>(s, p_p, w + 1, n, scr, 2, wm ? wm + 1 : nullptr);
       CK(cudaStreamSynchronize(s->stream));
     });
     return kernel_error(s);
@@ -1133,19 +1162,21 @@ int ttsh_get_provisional(ttsh_sim* s, int inst, double* ustar, double* Pstar) {
           if (s->fused) {  // the last step's u*, P*, compensated (the halves of the pairs)
             const float* sh = reinterpret_cast<const float*>(I.star[s->par][b]);
             const __nv_bfloat16* sl = reinterpret_cast<const __nv_bfloat16*>(I.starlo[s->par][b]);
-            if (ustar) {
-              launch_join(sh, sl, nullptr, scr, n, 2, s->stream);
-              CK(cudaMemcpyAsync(ustar + b * n, scr, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-            }
-            if (Pstar) {
-              launch_join(sh + 1, sl + 1, nullptr, scr, n, 2, s->stream);
-              CK(cudaMemcpyAsync(Pstar + b * n, scr, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-            }
+            auto get2 = [&](double* dst, const float* hi, const __nv_bfloat16* lo) {  // one half of the pairs
+              if (host_direct(s, dst, n * sizeof(double))) {
+                launch_join(hi, lo, nullptr, dst, n, 2, s->stream);
+                return;
+              }
+              launch_join(hi, lo, nullptr, scr, n, 2, s->stream);
+              CK(cudaMemcpyAsync(dst, scr, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+            };
+            if (ustar) get2(ustar + b * n, sh, sl);
+            if (Pstar) get2(Pstar + b * n, sh + 1, sl + 1);
             continue;
           }
         }
-        if (ustar) d2h<TT>(ustar + b * n, I.Us[s->par][b], n, s->stream, scr);
-        if (Pstar) d2h<TT>(Pstar + b * n, I.Ps[s->par][b], n, s->stream, scr);
+        if (ustar) d2h<TT>(s, ustar + b * n, I.Us[s->par][b], n, scr);
+        if (Pstar) d2h<TT>(s, Pstar + b * n, I.Ps[s->par][b], n, scr);
       }
       CK(cudaStreamSynchronize(s->stream));
     });
@@ -1307,10 +1338,10 @@ int ttsh_write_conf_async(ttsh_sim* s, int inst, const char* path) {
             launch_join(I.P[b], nullptr, nullptr, P + b * n, n, 1, s->stream);
           }
         } else {
-          launch_to_f64(I.phi[s->par], 1, phi, n, 1.0, s->stream);
+          launch_to_f64(I.phi[s->par], 1, phi, n, nullptr, s->stream);
           for (int b = 0; b < 3; ++b) {
-            launch_to_f64(I.U[b], 1, u + b * n, n, 1.0, s->stream);
-            launch_to_f64(I.P[b], 1, P + b * n, n, 1.0, s->stream);
+            launch_to_f64(I.U[b], 1, u + b * n, n, nullptr, s->stream);
+            launch_to_f64(I.P[b], 1, P + b * n, n, nullptr, s->stream);
           }
         }
       } else {

@@ -75,7 +75,10 @@ void fused_prepare();
 // FP64 <-> FP32 field conversion on the device (post.cu): dst[i] = src[i] and
 // dst[i] = src[i * stride] * scale (an exact power of two).
 void launch_to_f32(const double* src, float* dst, size_t n, cudaStream_t st);
-void launch_to_f64(const float* src, size_t stride, double* dst, size_t n, double scale, cudaStream_t st);
+// scale_bits: the float bits of the maximum whose power of two (pow2_denorm) scales the values
+// (device memory; nullptr: no scaling)
+void launch_to_f64(const float* src, size_t stride, double* dst, size_t n, const int* scale_bits, cudaStream_t st);
+void launch_gather_f64(const double* src, size_t stride, double* dst, size_t n, cudaStream_t st);
 // The fused FP32 form's compensated fields (post.cu): an FP64 field split into its FP32 value and
 // the remainder (bf16 lo or FP32 lo32), and joined back; hi and lo strided (2: one half of a pair
 // field).

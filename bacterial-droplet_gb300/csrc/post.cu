@@ -86,15 +86,24 @@ __global__ void k_slice(const InstDev<T>* __restrict__ insts, int inst, int par,
 }
 
 // FP64 <-> FP32 conversion of one field on the device, for the host interface of the FP32 forms:
-// the caller's FP64 arrays are copied as they are and converted here (round to nearest), instead
-// of being converted element by element on the host.
+// the caller's FP64 arrays are read (or written) as they are, in device memory or straight in
+// host memory the device can address, and converted here (round to nearest), instead of element
+// by element on the host. k_to_f64 multiplies by the power of two whose float bits *scale_bits
+// record (pow2_denorm; nullptr: 1), read on the device so that no host wait is needed for it.
 __global__ void k_to_f32(const double* __restrict__ src, float* __restrict__ dst, size_t n) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     dst[i] = __double2float_rn(src[i]);
 }
-__global__ void k_to_f64(const float* __restrict__ src, size_t stride, double* __restrict__ dst, size_t n, double scale) {
+__global__ void k_to_f64(const float* __restrict__ src, size_t stride, double* __restrict__ dst, size_t n,
+                         const int* __restrict__ scale_bits) {
+  const double scale = scale_bits ? (double)pow2_denorm(*scale_bits) : 1.0;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     dst[i] = (double)src[i * stride] * scale;
+}
+// a strided FP64 field (p_v or p_p of the packed complex W) into a contiguous one
+__global__ void k_gather_f64(const double* __restrict__ src, size_t stride, double* __restrict__ dst, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = src[i * stride];
 }
 
 // The compensated fields of the fused FP32 form: hi = the FP64 value rounded to FP32 and the
@@ -143,10 +152,14 @@ void launch_to_f32(const double* src, float* dst, size_t n, cudaStream_t st) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) throw std::runtime_error(std::string("conversion launch: ") + cudaGetErrorString(e));
 }
-void launch_to_f64(const float* src, size_t stride, double* dst, size_t n, double scale, cudaStream_t st) {
-  k_to_f64<<<1216, 256, 0, st>>>(src, stride, dst, n, scale);
+void launch_to_f64(const float* src, size_t stride, double* dst, size_t n, const int* scale_bits, cudaStream_t st) {
+  k_to_f64<<<1216, 256, 0, st>>>(src, stride, dst, n, scale_bits);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) throw std::runtime_error(std::string("conversion launch: ") + cudaGetErrorString(e));
+}
+void launch_gather_f64(const double* src, size_t stride, double* dst, size_t n, cudaStream_t st) {
+  k_gather_f64<<<1216, 256, 0, st>>>(src, stride, dst, n);
+  check_conv("gather");
 }
 
 int centroid_blocks() { return CB; }
