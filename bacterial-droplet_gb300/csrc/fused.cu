@@ -56,12 +56,19 @@ constexpr int NT = TX * TYR;      // threads of fused_rhs: one tile column each 
 constexpr int US = 4;             // strip length of the velocity terms (phase 1)
 
 // fused_rhs regions: A = tile + 2 (phi, P), B = tile + 1 (u, stage-1 products), C = tile.
-constexpr int AW = TX + 4, AH = TYR + 4, AN = AW * AH;
+constexpr int AH = TYR + 4;
 constexpr int BW = TX + 2, BH = TYR + 2, BN = BW * BH;
+// The staged state planes are planar (one array per field), rows of SXW floats from x0 - 4 to
+// x0 + TX + 3, copied in 16-byte chunks (4 sites): a chunk starts at a multiple of 4, so it never
+// straddles the periodic boundary and the copies are whole aligned segments. The A ring holds
+// (phi, Px, Py, Pz) over rows y0 - 2 .. y0 + TYR + 1, the u ring (ux, uy, uz) over rows
+// y0 - 1 .. y0 + TYR. Column of x: x - x0 + 4.
+constexpr int SXW = TX + 8, SXC = SXW / 4;
+constexpr int AFP = SXW * AH;  // floats per field plane, A ring
+constexpr int UFP = SXW * BH;  // floats per field plane, u ring
 constexpr int CN = TX * TY;  // fused_correct's tile
-// Row pitches in shared memory, one element longer than the rows: warps whose lanes sit in
+// Row pitches of the products, one element longer than the rows: warps whose lanes sit in
 // different rows (the stage-1 strips of the last two B columns) then hit different banks.
-constexpr int AP = AW + 1, ANP = AP * AH;  // A region (float2 pairs)
 constexpr int BP = BW + 1, BNP = BP * BH;  // B region
 constexpr int CP = TX + 1, CNP = CP * TYR;  // the tile (partials)
 // Products of one plane on B, as float2 pairs (plus one scalar field):
@@ -72,20 +79,23 @@ constexpr int PM0 = 0, PM1 = 1, PT0 = 2, PT1 = 3, PT2 = 4, PT3 = 5, NPR = 6;
 // Pointwise parts of the update on C ("partials"), float2 pairs:
 //   Q0 = (u_x, u_y) terms, Q1 = (u_z term, phi term), Q2 = (P_x, P_y) terms, Q3 = (P_z term, -)
 constexpr int NPQ = 4;
-// Shared memory (bytes): A ring RA planes x 2 pairs; u ring RU planes x ((ux, uy) pair + uz);
-// one plane of products; partials ring 2 planes. The A and u rings hold one plane more than the
-// stencils read: the next plane is copied into it (cp.async) while the current ones compute.
+// Shared memory (bytes): A ring RA planes x 4 fields; u ring RU planes x 3 fields; one plane of
+// products; partials ring 2 planes. The A and u rings hold one plane more than the stencils
+// read: the next plane is copied into it (cp.async) while the current ones compute.
 constexpr int RA = 4, RU = 4;
 constexpr size_t OFF_A = 0;
-constexpr size_t OFF_U01 = OFF_A + (size_t)RA * 2 * ANP * sizeof(float2);
-constexpr size_t OFF_U2 = OFF_U01 + (size_t)RU * BNP * sizeof(float2);
-constexpr size_t OFF_PR = OFF_U2 + (((size_t)RU * BNP * sizeof(float) + 15) / 16) * 16;
+constexpr size_t OFF_U = OFF_A + (size_t)RA * 4 * AFP * sizeof(float);
+constexpr size_t OFF_PR = OFF_U + (size_t)RU * 3 * UFP * sizeof(float);
 constexpr size_t OFF_SZX = OFF_PR + (size_t)NPR * BNP * sizeof(float2);
 constexpr size_t OFF_PQ = OFF_SZX + (((size_t)BNP * sizeof(float) + 15) / 16) * 16;
 constexpr size_t RHS_SMEM = OFF_PQ + (size_t)2 * NPQ * CNP * sizeof(float2);
 static_assert(2 * RHS_SMEM <= 227 * 1024, "fused_rhs: two CTAs per SM");
-static_assert(OFF_U01 % 16 == 0 && OFF_U2 % 16 == 0 && OFF_PR % 16 == 0 && OFF_SZX % 16 == 0 && OFF_PQ % 16 == 0,
-              "16-byte aligned regions");
+static_assert(OFF_U % 16 == 0 && OFF_PR % 16 == 0 && OFF_SZX % 16 == 0 && OFF_PQ % 16 == 0 &&
+                  (AFP * sizeof(float)) % 16 == 0 && (UFP * sizeof(float)) % 16 == 0 && (SXW * sizeof(float)) % 16 == 0,
+              "16-byte aligned regions, field planes and rows");
+// copy roles: (row, chunk) items of the A region, then of the u region, one thread each
+constexpr int NIA = AH * SXC, NIU = BH * SXC;
+static_assert(NIA + NIU <= NT, "one staged (row, chunk) item per thread");
 // phase-1 thread roles of fused_rhs: stage-1 strips of the B region, then the velocity strips
 constexpr int NS1 = (BW * BH) / RB;                   // 204 stage-1 strips
 constexpr int NU0 = ((NS1 + 31) / 32) * 32;           // first velocity thread (warp aligned)
@@ -99,6 +109,10 @@ __device__ __forceinline__ int wrapN(int a, int N) { return a < 0 ? a + N : (a >
 __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
@@ -227,9 +241,8 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
   float amu = 0.f, amp = 0.f;  // max |u*|, |P*| of this thread's outputs (the divergence's grid)
   float* const ophi = I.phi[par ^ 1];
   float* const phic = I.phic;
-  float2* const sA = reinterpret_cast<float2*>(smr + OFF_A);      // [RA][2][ANP]: (phi, Px), (Py, Pz)
-  float2* const sU01 = reinterpret_cast<float2*>(smr + OFF_U01);  // [RU][BNP]: (ux, uy)
-  float* const sU2 = reinterpret_cast<float*>(smr + OFF_U2);      // [RU][BNP]: uz
+  float* const sA = reinterpret_cast<float*>(smr + OFF_A);        // [RA][4][AFP]: phi, Px, Py, Pz
+  float* const sU = reinterpret_cast<float*>(smr + OFF_U);        // [RU][3][UFP]: ux, uy, uz
   float2* const sPr = reinterpret_cast<float2*>(smr + OFF_PR);    // [NPR][BNP]
   float* const sSzx = reinterpret_cast<float*>(smr + OFF_SZX);    // [BNP]
   float2* const sQ = reinterpret_cast<float2*>(smr + OFF_PQ);     // [2][NPQ][CNP]
@@ -239,51 +252,31 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
   // issue(i): A plane a = z0 - 2 + i (phi, P over tile+2) into A slot i % RA, and u plane a - 1
   // (tile+1) into u slot i % RU. Iteration i runs stage 1 at plane b = a - 1 and finishes plane
   // c = a - 2; issue(i + 1) runs during iteration i.
-  // Offsets within a plane of the elements this thread copies (t = tid + k NT of the A region,
-  // tile+2, and of the B region, tile+1), with the periodic wrap: the same for every plane.
-  constexpr int KA = (AN + NT - 1) / NT, KB = (BN + NT - 1) / NT;
-  // (and their shared-memory index in the padded rows)
-  int offA[KA], offB[KB], sidA[KA], sidB[KB];
-#pragma unroll
-  for (int k = 0; k < KA; ++k) {
-    const int t = tid + k * NT;
-    offA[k] = t < AN ? wrapN(y0 - 2 + t / AW, N) * N + wrapN(x0 - 2 + t % AW, N) : 0;
-    sidA[k] = t + t / AW;
-  }
-#pragma unroll
-  for (int k = 0; k < KB; ++k) {
-    const int t = tid + k * NT;
-    offB[k] = t < BN ? wrapN(y0 - 1 + t / BW, N) * N + wrapN(x0 - 1 + t % BW, N) : 0;
-    sidB[k] = t + t / BW;
+  // Thread tid < NIA copies (row, chunk) item tid of the A region for its 4 fields, thread
+  // NIA <= tid < NIA + NIU item tid - NIA of the u region for its 3; the offsets within a plane
+  // (periodic wrap included) are the same for every plane.
+  const bool cpA = tid < NIA, cpU = !cpA && tid < NIA + NIU;
+  int goff = 0, soff = 0;
+  if (cpA || cpU) {
+    const int t = cpA ? tid : tid - NIA;
+    const int row = t / SXC, ch = t - row * SXC;
+    goff = wrapN((cpA ? y0 - 2 : y0 - 1) + row, N) * N + wrapN(x0 - 4 + 4 * ch, N);
+    soff = row * SXW + 4 * ch;
   }
   auto issue = [&](int i) {
-    const size_t za = (size_t)wrapN(z0 - 2 + i, N) * NN;
-    float* dst = reinterpret_cast<float*>(sA + (i % RA) * 2 * ANP);
-#pragma unroll
-    for (int k = 0; k < KA; ++k) {
-      const int t = tid + k * NT;
-      if (t < AN) {
-        const size_t g = za + offA[k];
-        const int d = sidA[k];
-        cp_async4(dst + 2 * d, gphi + g);
-        cp_async4(dst + 2 * d + 1, gP[0] + g);
-        cp_async4(dst + 2 * (ANP + d), gP[1] + g);
-        cp_async4(dst + 2 * (ANP + d) + 1, gP[2] + g);
-      }
-    }
-    const size_t zu = (size_t)wrapN(z0 - 3 + i, N) * NN;
-    float* du = reinterpret_cast<float*>(sU01 + (i % RU) * BNP);
-    float* dz = sU2 + (i % RU) * BNP;
-#pragma unroll
-    for (int k = 0; k < KB; ++k) {
-      const int t = tid + k * NT;
-      if (t < BN) {
-        const size_t g = zu + offB[k];
-        const int d = sidB[k];
-        cp_async4(du + 2 * d, gU[0] + g);
-        cp_async4(du + 2 * d + 1, gU[1] + g);
-        cp_async4(dz + d, gU[2] + g);
-      }
+    if (cpA) {
+      const size_t d = (size_t)wrapN(z0 - 2 + i, N) * NN + goff;
+      float* dst = sA + (i % RA) * 4 * AFP + soff;
+      cp_async16(dst, gphi + d);
+      cp_async16(dst + AFP, gP[0] + d);
+      cp_async16(dst + 2 * AFP, gP[1] + d);
+      cp_async16(dst + 3 * AFP, gP[2] + d);
+    } else if (cpU) {
+      const size_t d = (size_t)wrapN(z0 - 3 + i, N) * NN + goff;
+      float* dst = sU + (i % RU) * 3 * UFP + soff;
+      cp_async16(dst, gU[0] + d);
+      cp_async16(dst + UFP, gU[1] + d);
+      cp_async16(dst + 2 * UFP, gU[2] + d);
     }
     cp_async_commit();
   };
@@ -333,9 +326,9 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
     // ---- phase 1a, stage 1 at plane b = z0 - 3 + i over B (tile+1): the products mu_0, mu_b,
     //      S_ab that phase 2 differentiates, and on the tile the pointwise parts of the update
     if (i >= 2 && tid < NS1) {
-      const float2* a0 = sA + ((i + RA - 2) % RA) * 2 * ANP;  // plane b-1
-      const float2* a1 = sA + ((i + RA - 1) % RA) * 2 * ANP;  // plane b
-      const float2* a2 = sA + (i % RA) * 2 * ANP;             // plane b+1
+      const float* a0 = sA + ((i + RA - 2) % RA) * 4 * AFP;  // plane b-1
+      const float* a1 = sA + ((i + RA - 1) % RA) * 4 * AFP;  // plane b
+      const float* a2 = sA + (i % RA) * 4 * AFP;             // plane b+1
       // strips of the B region: warps take 32 consecutive columns of one strip row (unit-stride
       // shared-memory access); the last BW - 32 columns of every row come after them
       constexpr int NSR = BH / RB, NMAIN = 32 * NSR;
@@ -343,25 +336,25 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
       int bx, by0;
       if (s < NMAIN) { bx = s & 31; by0 = (s >> 5) * RB; }
       else { const int e = s - NMAIN; bx = 32 + e % (BW - 32); by0 = (e / (BW - 32)) * RB; }
-      const int base = by0 * AP + bx;  // A index of row offset -1, column offset -1 of site 0
+      // A index of row offset -1, column offset -1 of site 0 (B column bx is x = x0 - 1 + bx)
+      const int base = by0 * SXW + bx + 2;
       // pair 0 = (phi, Px), pair 1 = (Py, Pz): D_a (3), L and the centre value of each site
       float2 D0[3][RB], L0[RB], C0[RB], D1[3][RB], L1[RB], C1[RB];
       {
         auto ld = [&](int z, int r, int c) {
-          const float2* pl = z == 0 ? a0 : (z == 1 ? a1 : a2);
-          return pl[base + r * AP + c];
+          const float* pl = (z == 0 ? a0 : (z == 1 ? a1 : a2)) + base + r * SXW + c;
+          return f2(pl[0], pl[AFP]);
         };
         sep_rows<RB, true, true, true, true, float2>(ld, sk, D0[0], D0[1], D0[2], L0, C0);
       }
       {
         auto ld = [&](int z, int r, int c) {
-          const float2* pl = z == 0 ? a0 : (z == 1 ? a1 : a2);
-          return pl[ANP + base + r * AP + c];
+          const float* pl = (z == 0 ? a0 : (z == 1 ? a1 : a2)) + base + r * SXW + c;
+          return f2(pl[2 * AFP], pl[3 * AFP]);
         };
         sep_rows<RB, true, true, true, true, float2>(ld, sk, D1[0], D1[1], D1[2], L1, C1);
       }
-      const float2* ubp = sU01 + (i % RU) * BNP;  // u at plane b
-      const float* ubz = sU2 + (i % RU) * BNP;
+      const float* ub = sU + (i % RU) * 3 * UFP;  // u at plane b
       float2* pq = sQ + (i & 1) * NPQ * CNP;
 #pragma unroll
       for (int k = 0; k < RB; ++k) {
@@ -394,8 +387,8 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
           //   P_b:  -(u + lambda0 P).D P_b - P_b (alpha phi + beta |P|^2 + A |D phi|^2 |P|^2)
           //         - A |P| (D phi . P) D_b phi
           const int c = cy * CP + cx;
-          const float2 uxy = ubp[o];
-          const float vx = uxy.x, vy = uxy.y, vz = ubz[o];
+          const int ou = (by0 + k) * SXW + bx + 3;
+          const float vx = ub[ou], vy = ub[UFP + ou], vz = ub[2 * UFP + ou];
           const float mu0 = M0.x;
           const float gx = D0[0][k].x, gy = D0[1][k].x, gz = D0[2][k].x;  // D phi
           const float P2 = px * px + py * py + pz * pz;
@@ -424,20 +417,21 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
       const int s = tid - NU0;
       const int vx = s & 31, vy0 = (s >> 5) * US;  // tile coordinates of the strip
       const int sl0 = (i + RU - 2) % RU, sl1 = (i + RU - 1) % RU, sl2 = i % RU;  // planes c-1, c, c+1
-      const int base = vy0 * BP + vx;  // B index of row offset -1, column offset -1 of site 0
+      const int base = vy0 * SXW + vx + 3;  // u index of row offset -1, column offset -1 of site 0
       float2 Dp[3][US], Lp[US], Cp[US];
       float Dz[3][US], Lz[US], Cz[US];
       {
         auto ld = [&](int z, int r, int c) {
           const int sl = z == 0 ? sl0 : (z == 1 ? sl1 : sl2);
-          return sU01[sl * BNP + base + r * BP + c];
+          const float* pl = sU + sl * 3 * UFP + base + r * SXW + c;
+          return f2(pl[0], pl[UFP]);
         };
         sep_rows<US, true, true, true, true, float2>(ld, sk, Dp[0], Dp[1], Dp[2], Lp, Cp);
       }
       {
         auto ld = [&](int z, int r, int c) {
           const int sl = z == 0 ? sl0 : (z == 1 ? sl1 : sl2);
-          return sU2[sl * BNP + base + r * BP + c];
+          return sU[sl * 3 * UFP + 2 * UFP + base + r * SXW + c];
         };
         sep_rows<US, true, true, true, true, float>(ld, sk, Dz[0], Dz[1], Dz[2], Lz, Cz);
       }
@@ -461,8 +455,8 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
     if (i >= 2) {
       const int zc = z0 - 4 + i;
       const float2* pq = sQ + ((i + 1) & 1) * NPQ * CNP;    // plane c: stage 1 + velocity terms
-      const int sl = (i + RU - 1) % RU;                     // u at plane c
-      const float2* ac = sA + ((i + RA - 2) % RA) * 2 * ANP;  // phi, P at plane c
+      const float* uc = sU + ((i + RU - 1) % RU) * 3 * UFP;  // u at plane c
+      const float* ac = sA + ((i + RA - 2) % RA) * 4 * AFP;  // phi, P at plane c
       const float2 four = f2(4.f, 4.f);
       if (halfA) {
         float2 lm[2][2];  // [site]: (L mu_0, L mu_x), (L mu_y, L mu_z)
@@ -524,12 +518,12 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
         if (i >= 4) {
 #pragma unroll
           for (int k = 0; k < 2; ++k) {
-            const int c = (py0 + k) * CP + px, oa = (py0 + k + 2) * AP + (px + 2), ob = (py0 + k + 1) * BP + (px + 1);
+            const int c = (py0 + k) * CP + px, oa = (py0 + k + 2) * SXW + (px + 4), ou = (py0 + k + 1) * SXW + (px + 4);
             const size_t g = (size_t)zc * NN + (size_t)(y0 + py0 + k) * N + (x0 + px);
             const float2 q0 = pq[0 * CNP + c], q1 = pq[1 * CNP + c], q2 = pq[2 * CNP + c], q3 = pq[3 * CNP + c];
-            const float2 A0 = ac[oa], A1 = ac[ANP + oa];
+            const float2 A0 = f2(ac[oa], ac[AFP + oa]), A1 = f2(ac[2 * AFP + oa], ac[3 * AFP + oa]);
             // u*_x = u_x + dt d/dt u_x (:480-482)
-            const float usx = put_comp(oUs[0], oSlo[0], g, sU01[sl * BNP + ob].x, p.dt * fmaf(sk.d, dvx[k], q0.x),
+            const float usx = put_comp(oUs[0], oSlo[0], g, uc[ou], p.dt * fmaf(sk.d, dvx[k], q0.x),
                                        lprev[k][0], 2);
             // P*_b = P_b + dt (pointwise part + eta L mu_b) (:623-629, :486-488)
             const float psx = put_comp(oPs[0], oSlo[3], g, A0.y, p.dt * fmaf(p.eta, lm[k][0].y, q2.x), lprev[k][1], 2);
@@ -587,13 +581,13 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
         if (i >= 4) {
 #pragma unroll
           for (int k = 0; k < 2; ++k) {
-            const int c = (py0 + k) * CP + px, ob = (py0 + k + 1) * BP + (px + 1);
+            const int c = (py0 + k) * CP + px, ou = (py0 + k + 1) * SXW + (px + 4);
             const size_t g = (size_t)zc * NN + (size_t)(y0 + py0 + k) * N + (x0 + px);
             const float2 q0 = pq[0 * CNP + c], q1 = pq[1 * CNP + c];
             // (u*_y, u*_z) = (u_y, u_z) + dt d/dt (u_y, u_z) (:480-482)
             const float2 du = vmul(vsplat(p.dt, float2()), vfma(vsplat(sk.d, float2()), dv[k], f2(q0.y, q1.x)));
-            const float usy = put_comp(oUs[1], oSlo[1], g, sU01[sl * BNP + ob].y, du.x, lprev[k][0], 2);
-            const float usz = put_comp(oUs[2], oSlo[2], g, sU2[sl * BNP + ob], du.y, lprev[k][1], 2);
+            const float usy = put_comp(oUs[1], oSlo[1], g, uc[UFP + ou], du.x, lprev[k][0], 2);
+            const float usz = put_comp(oUs[2], oSlo[2], g, uc[2 * UFP + ou], du.y, lprev[k][1], 2);
             amu = fmaxf(amu, fmaxf(fabsf(usy), fabsf(usz)));
           }
         }
@@ -664,11 +658,6 @@ constexpr size_t COR_SMEM = DR * COR_SLOT;
 // wait until at most DR - 2 copy groups are pending: the group of the plane read now is complete
 __device__ __forceinline__ void cp_async_wait_ring() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(DR - 2) : "memory");
-}
-
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 
 // fused_div: 4-site strips of a 32 x 32 tile (a 6 x 3 window of each staged field serves the
