@@ -57,15 +57,19 @@ constexpr int US = 4;             // strip length of the velocity terms (phase 1
 
 // fused_rhs regions: A = tile + 2 (phi, P), B = tile + 1 (u, stage-1 products), C = tile.
 constexpr int AH = TYR + 4;
-constexpr int BW = TX + 2, BH = TYR + 2, BN = BW * BH;
+constexpr int BW = TX + 2, BH = TYR + 2;
 // The staged state planes are planar (one array per field), rows of SXW floats from x0 - 4 to
 // x0 + TX + 3, copied in 16-byte chunks (4 sites): a chunk starts at a multiple of 4, so it never
 // straddles the periodic boundary and the copies are whole aligned segments. The A ring holds
 // (phi, Px, Py, Pz) over rows y0 - 2 .. y0 + TYR + 1, the u ring (ux, uy, uz) over rows
-// y0 - 1 .. y0 + TYR. Column of x: x - x0 + 4.
+// y0 - 1 .. y0 + TYR. Column of x: x - x0 + 4. Staged row r starts at srow(r): every second row
+// is skewed by one more chunk, so that the stage-1 strips of the last two B columns (rows
+// 0, 2, .., 8 apart in one warp) read ten different banks; strips start at even rows, so a
+// window row's offset from its strip's first row is srow(r) too.
 constexpr int SXW = TX + 8, SXC = SXW / 4;
-constexpr int AFP = SXW * AH;  // floats per field plane, A ring
-constexpr int UFP = SXW * BH;  // floats per field plane, u ring
+__host__ __device__ constexpr int srow(int r) { return r * SXW + 4 * (r >> 1); }
+constexpr int AFP = srow(AH - 1) + SXW;  // floats per field plane, A ring
+constexpr int UFP = srow(BH - 1) + SXW;  // floats per field plane, u ring
 constexpr int CN = TX * TY;  // fused_correct's tile
 // Row pitches of the products, one element longer than the rows: warps whose lanes sit in
 // different rows (the stage-1 strips of the last two B columns) then hit different banks.
@@ -106,10 +110,6 @@ static_assert(NU0 + NUS <= NT, "phase-1 roles fit the block");
 __device__ __forceinline__ int wrapN(int a, int N) { return a < 0 ? a + N : (a >= N ? a - N : a); }
 
 // Asynchronous global -> shared copies (cp.async): the data lands while the CTA computes.
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
-}
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
@@ -261,7 +261,7 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
     const int t = cpA ? tid : tid - NIA;
     const int row = t / SXC, ch = t - row * SXC;
     goff = wrapN((cpA ? y0 - 2 : y0 - 1) + row, N) * N + wrapN(x0 - 4 + 4 * ch, N);
-    soff = row * SXW + 4 * ch;
+    soff = srow(row) + 4 * ch;
   }
   auto issue = [&](int i) {
     if (cpA) {
@@ -337,19 +337,19 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
       if (s < NMAIN) { bx = s & 31; by0 = (s >> 5) * RB; }
       else { const int e = s - NMAIN; bx = 32 + e % (BW - 32); by0 = (e / (BW - 32)) * RB; }
       // A index of row offset -1, column offset -1 of site 0 (B column bx is x = x0 - 1 + bx)
-      const int base = by0 * SXW + bx + 2;
+      const int base = srow(by0) + bx + 2;
       // pair 0 = (phi, Px), pair 1 = (Py, Pz): D_a (3), L and the centre value of each site
       float2 D0[3][RB], L0[RB], C0[RB], D1[3][RB], L1[RB], C1[RB];
       {
         auto ld = [&](int z, int r, int c) {
-          const float* pl = (z == 0 ? a0 : (z == 1 ? a1 : a2)) + base + r * SXW + c;
+          const float* pl = (z == 0 ? a0 : (z == 1 ? a1 : a2)) + base + srow(r) + c;
           return f2(pl[0], pl[AFP]);
         };
         sep_rows<RB, true, true, true, true, float2>(ld, sk, D0[0], D0[1], D0[2], L0, C0);
       }
       {
         auto ld = [&](int z, int r, int c) {
-          const float* pl = (z == 0 ? a0 : (z == 1 ? a1 : a2)) + base + r * SXW + c;
+          const float* pl = (z == 0 ? a0 : (z == 1 ? a1 : a2)) + base + srow(r) + c;
           return f2(pl[2 * AFP], pl[3 * AFP]);
         };
         sep_rows<RB, true, true, true, true, float2>(ld, sk, D1[0], D1[1], D1[2], L1, C1);
@@ -387,7 +387,7 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
           //   P_b:  -(u + lambda0 P).D P_b - P_b (alpha phi + beta |P|^2 + A |D phi|^2 |P|^2)
           //         - A |P| (D phi . P) D_b phi
           const int c = cy * CP + cx;
-          const int ou = (by0 + k) * SXW + bx + 3;
+          const int ou = srow(by0 + k) + bx + 3;
           const float vx = ub[ou], vy = ub[UFP + ou], vz = ub[2 * UFP + ou];
           const float mu0 = M0.x;
           const float gx = D0[0][k].x, gy = D0[1][k].x, gz = D0[2][k].x;  // D phi
@@ -417,13 +417,13 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
       const int s = tid - NU0;
       const int vx = s & 31, vy0 = (s >> 5) * US;  // tile coordinates of the strip
       const int sl0 = (i + RU - 2) % RU, sl1 = (i + RU - 1) % RU, sl2 = i % RU;  // planes c-1, c, c+1
-      const int base = vy0 * SXW + vx + 3;  // u index of row offset -1, column offset -1 of site 0
+      const int base = srow(vy0) + vx + 3;  // u index of row offset -1, column offset -1 of site 0
       float2 Dp[3][US], Lp[US], Cp[US];
       float Dz[3][US], Lz[US], Cz[US];
       {
         auto ld = [&](int z, int r, int c) {
           const int sl = z == 0 ? sl0 : (z == 1 ? sl1 : sl2);
-          const float* pl = sU + sl * 3 * UFP + base + r * SXW + c;
+          const float* pl = sU + sl * 3 * UFP + base + srow(r) + c;
           return f2(pl[0], pl[UFP]);
         };
         sep_rows<US, true, true, true, true, float2>(ld, sk, Dp[0], Dp[1], Dp[2], Lp, Cp);
@@ -431,7 +431,7 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
       {
         auto ld = [&](int z, int r, int c) {
           const int sl = z == 0 ? sl0 : (z == 1 ? sl1 : sl2);
-          return sU[sl * 3 * UFP + 2 * UFP + base + r * SXW + c];
+          return sU[sl * 3 * UFP + 2 * UFP + base + srow(r) + c];
         };
         sep_rows<US, true, true, true, true, float>(ld, sk, Dz[0], Dz[1], Dz[2], Lz, Cz);
       }
@@ -518,7 +518,7 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
         if (i >= 4) {
 #pragma unroll
           for (int k = 0; k < 2; ++k) {
-            const int c = (py0 + k) * CP + px, oa = (py0 + k + 2) * SXW + (px + 4), ou = (py0 + k + 1) * SXW + (px + 4);
+            const int c = (py0 + k) * CP + px, oa = srow(py0 + k + 2) + (px + 4), ou = srow(py0 + k + 1) + (px + 4);
             const size_t g = (size_t)zc * NN + (size_t)(y0 + py0 + k) * N + (x0 + px);
             const float2 q0 = pq[0 * CNP + c], q1 = pq[1 * CNP + c], q2 = pq[2 * CNP + c], q3 = pq[3 * CNP + c];
             const float2 A0 = f2(ac[oa], ac[AFP + oa]), A1 = f2(ac[2 * AFP + oa], ac[3 * AFP + oa]);
@@ -581,7 +581,7 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
         if (i >= 4) {
 #pragma unroll
           for (int k = 0; k < 2; ++k) {
-            const int c = (py0 + k) * CP + px, ou = (py0 + k + 1) * SXW + (px + 4);
+            const int c = (py0 + k) * CP + px, ou = srow(py0 + k + 1) + (px + 4);
             const size_t g = (size_t)zc * NN + (size_t)(y0 + py0 + k) * N + (x0 + px);
             const float2 q0 = pq[0 * CNP + c], q1 = pq[1 * CNP + c];
             // (u*_y, u*_z) = (u_y, u_z) + dt d/dt (u_y, u_z) (:480-482)
