@@ -244,6 +244,88 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_snapshot(args):
+    """--snapshot: the snapshot writer (conf_<te>.dat, ExpoConf's text layout) in text bytes per
+    second at N^3, ours (synchronous ttsh_write_conf, and ttsh_write_conf_async issued before K
+    steps: the host time it takes and how much of its formatting the steps hide) against the
+    reference program's own ExpoConf (TTSH3D.cu:899-1014: 58 device-to-host copies, then one line
+    per site through ofstream with endl). The reference's time is the difference of two runs of
+    its timed step loop (warm-up 1, steps 2-4): one with a snapshot at step 3, one without."""
+    import shutil
+    import ttsh
+    N, K = args.snapshot_n, args.steps
+    out = {"metric": "snapshot text bytes/s", "unit": "MB/s", "n": N, "impl": "snapshot"}
+    base = tempfile.mkdtemp(prefix="ttsh_conf_")
+    try:
+        free = shutil.disk_usage(base).free
+        need = 3 * 125 * N ** 3 + 15 * 8 * N ** 3
+        if free < need:
+            raise SystemExit("snapshot bench: %d bytes free under %s, %d needed" % (free, base, need))
+        phi, P = ttsh.init_droplet(N, N / 4.0, 2.0, 1)
+        inp = ttsh.default_input(Nx=N, Ny=N, Nz=N)
+        with ttsh.Sim(inp, ttsh.default_ext(precision=32, zeta=0.02, form=ttsh.FORM_FUSED)) as s:
+            s.set_state(0, phi, P, np.zeros_like(P))
+            s.step(3)
+            s.sync()
+            path = os.path.join(base, "conf_1.dat")
+            t0 = time.perf_counter()
+            s.write_conf(0, path)
+            t1 = time.perf_counter()
+            nbytes = os.path.getsize(path)
+            os.remove(path)
+            s.sync()
+            t2 = time.perf_counter()
+            s.step(K)
+            s.sync()
+            t3 = time.perf_counter()
+            s.write_conf_async(0, path)
+            t4 = time.perf_counter()
+            s.step(K)
+            s.sync()
+            t5 = time.perf_counter()
+            s.conf_wait()
+            t6 = time.perf_counter()
+            assert os.path.getsize(path) == nbytes
+            os.remove(path)
+        out["ours"] = {"bytes": nbytes, "sync_s": t1 - t0, "sync_MBps": nbytes / (t1 - t0) / 1e6,
+                       "steps": K, "steps_alone_s": t3 - t2, "async_call_s": t4 - t3,
+                       "steps_after_async_s": t5 - t3, "async_total_s": t6 - t3,
+                       "exposed_s": (t6 - t3) - (t3 - t2),
+                       "form": "FP32 fused, 1 droplet, cores %d" % (os.cpu_count() or 0)}
+        try:
+            import make_ref
+            binary = make_ref.build()
+        except Exception as e:
+            binary = None
+            out["reference"] = {"unavailable": "reference program not built: %s" % str(e)[:200]}
+        if binary:
+            import make_ref_golden as G
+            import oracle
+            phi, P = oracle.init_droplet(N, N / 4.0, 2.0, 1)
+            st = {k: np.zeros((N, N, N)) for k in G.FIELDS}
+            st["phi"] = phi
+            st["px"], st["py"], st["pz"] = P
+            dt, T0 = 0.002, 1e-6
+            secs, sizes = [], []
+            for dte in (1e9, 2.5 * dt):  # no snapshot / one at step 3 (T = 3 dt + T0)
+                d = os.path.join(base, "ref_%g" % dte)
+                log = G.run_reference(binary, d, N, st, Ts=3.5 * dt, dte=dte, expo=1, warmup=1, nfields=7, T0=T0)
+                line = [l for l in log.splitlines() if l.startswith("TTSH_REF_TIMING")][-1]
+                kv = dict(x.split("=") for x in line.split()[1:])
+                secs.append(float(kv["seconds"]))
+                confs = [f for f in os.listdir(os.path.join(d, "data_1")) if f.startswith("conf_")]
+                sizes.append(sum(os.path.getsize(os.path.join(d, "data_1", f)) for f in confs))
+                shutil.rmtree(d, ignore_errors=True)
+            expo_s = secs[1] - secs[0]
+            out["reference"] = {"bytes": sizes[1], "loop_s_without": secs[0], "loop_s_with": secs[1],
+                                "expoconf_s": expo_s, "MBps": sizes[1] / expo_s / 1e6 if expo_s > 0 else None}
+            if out["reference"]["MBps"]:
+                out["sync_speedup"] = out["ours"]["sync_MBps"] / out["reference"]["MBps"]
+    finally:
+        shutil.rmtree(base, ignore_errors=True)
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -258,7 +340,13 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 one-droplet reference point")
     ap.add_argument("--no-tune", action="store_true", help="keep the default kernel configuration")
+    ap.add_argument("--snapshot", action="store_true",
+                    help="measure the snapshot writer (text bytes/s) against the reference's ExpoConf and exit")
+    ap.add_argument("--snapshot-n", type=int, default=256)
     args = ap.parse_args()
+    if args.snapshot:
+        run_snapshot(args)
+        return
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
 

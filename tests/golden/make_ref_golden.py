@@ -64,7 +64,7 @@ def read_bin(path):
 
 
 # Token positions in input.dat (run_cuda.pl:53-86, TTSH3D.cu:702-739) of the values the runs change.
-_POS = {"ExpoData": 4, "Nx": 8, "Ny": 9, "Nz": 10, "dt0": 13, "Ts": 15, "dte": 16}
+_POS = {"ExpoData": 4, "Nx": 8, "Ny": 9, "Nz": 10, "dt0": 13, "T0": 14, "Ts": 15, "dte": 16}
 
 
 def _perl_number(v):
@@ -75,21 +75,22 @@ def _perl_number(v):
     return s[:-2] if s.endswith(".0") else s
 
 
-def reference_input_text(N, Ts, dte, expo=1, dt0=0.002):
+def reference_input_text(N, Ts, dte, expo=1, dt0=0.002, T0=0):
     """input.dat for the reference program: the reference defaults (tests/golden/input_default.dat,
-    written by run_cuda.pl's own lines) with N, Ts, dte, ExpoData and dt0 replaced. Pure Python,
-    so that the timed reference arm loads nothing of libttsh."""
+    written by run_cuda.pl's own lines) with N, Ts, dte, ExpoData, dt0 and T0 replaced (T0 != 0:
+    no conf_0.dat before the loop, evolve :301-304). Pure Python, so that the timed reference arm
+    loads nothing of libttsh."""
     tok = open(os.path.join(ROOT, "tests", "golden", "input_default.dat")).read().split()
     for k, v in (("ExpoData", int(expo)), ("Nx", int(N)), ("Ny", int(N)), ("Nz", int(N)), ("dt0", float(dt0)),
-                 ("Ts", float(Ts)), ("dte", float(dte))):
+                 ("T0", T0), ("Ts", float(Ts)), ("dte", float(dte))):
         tok[_POS[k]] = _perl_number(v)
     return "\n".join(tok) + "\n"
 
 
-def run_reference(binary, workdir, N, st, Ts, dte, expo=1, warmup=0, nfields=15, timeout=3600):
+def run_reference(binary, workdir, N, st, Ts, dte, expo=1, warmup=0, nfields=15, timeout=3600, T0=0):
     os.makedirs(os.path.join(workdir, "data_1"), exist_ok=True)
     with open(os.path.join(workdir, "data_1", "input.dat"), "w") as fh:
-        fh.write(reference_input_text(N, Ts, dte, expo))
+        fh.write(reference_input_text(N, Ts, dte, expo, T0=T0))
     write_bin(os.path.join(workdir, "data_1", "init.bin"), st, N, nfields)
     env = dict(os.environ)
     env["TTSH_REF_WARMUP"] = str(warmup)
