@@ -138,7 +138,11 @@ int ttsh_step(ttsh_sim* s, int nsteps);
 int ttsh_sync(ttsh_sim* s);
 
 /* Device -> host copies of ExpoConf (TTSH3D.cu:904-963): any pointer may be NULL.
- * P, u, ustar, Pstar are 3*N^3; p_v and p_p are the last projection's pressures. */
+ * P, u, ustar, Pstar are 3*N^3; p_v and p_p are the last projection's pressures.
+ * Host arrays of ttsh_set_state / ttsh_get_state / ttsh_get_provisional in page-locked memory
+ * (cudaHostAlloc, cudaHostRegister, torch's pin_memory) are read and written in place by the
+ * device's conversion kernels; pageable arrays are staged through device memory by the copy
+ * engines. Both give the same values. */
 int ttsh_get_state(ttsh_sim* s, int inst, double* phi, double* P, double* u, double* p_v, double* p_p);
 int ttsh_get_provisional(ttsh_sim* s, int inst, double* ustar, double* Pstar);
 
