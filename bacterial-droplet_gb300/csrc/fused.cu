@@ -280,46 +280,46 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
     }
     cp_async_commit();
   };
-  // phase 2: four groups of 64 threads (two warps each), thread tid % 64 of a group on the 4-site
-  // strip of column px, rows py0 .. py0 + 3 of the tile, for one set of outer stencils:
-  //   group 0: the Laplacians of (mu_0, mu_x), then phi' and P*_x;
-  //   group 1: the Laplacians of (mu_y, mu_z), then P*_y, P*_z;
-  //   group 2: the divergence of stress column x (S_xx, S_yx; S_zx), then u*_x;
-  //   group 3: the divergence of stress columns (y, z), then u*_y, u*_z.
-  // Each group has every input of what it writes; the strip's four sites share a 6 x 3 window
-  // of each product plane.
-  constexpr int SP = 4;
-  static_assert(NT == 4 * TX * (TYR / SP), "phase 2: four groups of 4-site strips");
-  const int grp = tid / (NT / 4);
-  const int ps = tid % (NT / 4);
-  const int px = ps % TX, py0 = (ps / TX) * SP;
+  // phase 2: thread tid takes the 2-site strip s = tid % 256 of the tile (column px, rows py0,
+  // py0 + 1) for one half of the outer stencils: half A (tid < 256) the Laplacians of (mu_0, mu_x),
+  // (mu_y, mu_z) and the divergence of stress column x, then P*, phi' and u*_x; half B the
+  // divergence of stress columns (y, z), then u*_y, u*_z. Each half has every input of what it
+  // writes. The sites' rows share a 4 x 3 window of each product plane.
+  static_assert(NT == 2 * TX * (TYR / 2), "phase 2: two halves of 2-site strips");
+  const bool halfA = tid < NT / 2;
+  const int ps = tid & (NT / 2 - 1);
+  const int px = ps % TX, py0 = (ps / TX) * 2;
   const int pbase = py0 * BP + px;  // B index of window row 0 (site 0's row - 1), column px - 1 + 1 - 1
-  // z-combinations carried from plane to plane, per site k: for a Laplacian (groups 0, 1) the
-  // partial sum of the plane just finished + 1 and that of the plane after it (cv[k], cv[SP + k]);
-  // likewise for the divergences (group 3: float2 (y, z); group 2: the pair (rX1, rX2) in cv[k]).
-  float2 cv[2 * SP];
+  // z-combinations carried from plane to plane: for a Laplacian, the partial sum of the plane
+  // just finished + 1 and that of the plane after it (rL1, rL2); likewise for the divergences.
+  // Half A: cv2[0..3] = rL1 [site][pair], cv2[4..7] = rL2, cv1[0..1] = rX1 [site], cv1[2..3] = rX2;
+  // half B: cv2[0..1] = rD1 [site], cv2[2..3] = rD2.
+  float2 cv2[8];
+  float cv1[4];
 #pragma unroll
-  for (int k = 0; k < 2 * SP; ++k) cv[k] = f2(0.f, 0.f);
+  for (int k = 0; k < 8; ++k) cv2[k] = f2(0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) cv1[k] = 0.f;
   issue(0);
   for (int i = 0; i < niter; ++i) {
     cp_async_wait_all();
     __syncthreads();
     if (i + 1 < niter) issue(i + 1);
-    // the compensations of this iteration's output sites, loaded before phase 1 so that the
-    // phase-1 work covers the loads: phi's (group 0, float bits), u_x's (group 2), u_y's and u_z's
-    // (group 3, bf16 bits); P is an FP32 state (no compensation read)
-    unsigned pre[2 * SP];
+    // the compensations of this iteration's output sites (phi, u_x and P in half A; u_y, u_z in
+    // half B), loaded before phase 1 so that the phase-1 work covers the loads
+    float cprev[2] = {0.f, 0.f};
+    __nv_bfloat16 lprev[2][4];
     if (i >= 4) {
 #pragma unroll
-      for (int k = 0; k < SP; ++k) {
+      for (int k = 0; k < 2; ++k) {
         const size_t g = (size_t)(z0 - 4 + i) * NN + (size_t)(y0 + py0 + k) * N + (x0 + px);
-        if (grp == 0) {
-          pre[k] = __float_as_uint(phic[g]);
-        } else if (grp == 2) {
-          pre[k] = __bfloat16_as_ushort(I.lo[0][g]);
-        } else if (grp == 3) {
-          pre[k] = __bfloat16_as_ushort(I.lo[1][g]);
-          pre[SP + k] = __bfloat16_as_ushort(I.lo[2][g]);
+        if (halfA) {
+          cprev[k] = phic[g];
+          lprev[k][0] = I.lo[0][g];
+          lprev[k][1] = lprev[k][2] = lprev[k][3] = __float2bfloat16_rn(0.f);  // P: FP32 state
+        } else {
+          lprev[k][0] = I.lo[1][g];
+          lprev[k][1] = I.lo[2][g];
         }
       }
     }
@@ -454,163 +454,140 @@ __device__ __forceinline__ void rhs_segment(const InstDev<float>& I, int par, in
     //      b, carried in z; plane c = b - 1 is then complete
     if (i >= 2) {
       const int zc = z0 - 4 + i;
-      const float2* pq = sQ + ((i + 1) & 1) * NPQ * CNP;      // plane c: stage 1 + velocity terms
+      const float2* pq = sQ + ((i + 1) & 1) * NPQ * CNP;    // plane c: stage 1 + velocity terms
       const float* uc = sU + ((i + RU - 1) % RU) * 3 * UFP;  // u at plane c
       const float* ac = sA + ((i + RA - 2) % RA) * 4 * AFP;  // phi, P at plane c
       const float2 four = f2(4.f, 4.f);
-      const __nv_bfloat16 zero_lo = __float2bfloat16_rn(0.f);
-      if (grp < 2) {
-        // the Laplacians of the product pair (mu_0, mu_x) (group 0) or (mu_y, mu_z) (group 1):
-        // shift-invariant in-plane sums (see SepK): an off-centre plane adds
-        // G = l12 (4 diagonals - 4 centre) + lz centre, the centre plane
-        // H = l23 (4 edges - 4 centre) - 2 lz centre; G + H + G = L, zero for a constant field
-        const float2* F = sPr + (PM0 + grp) * BNP + pbase;
-        float2 v[SP + 2][3], rc[SP + 2];
+      if (halfA) {
+        float2 lm[2][2];  // [site]: (L mu_0, L mu_x), (L mu_y, L mu_z)
 #pragma unroll
-        for (int r = 0; r < SP + 2; ++r) {
+        for (int q = 0; q < 2; ++q) {
+          const float2* F = sPr + (PM0 + q) * BNP + pbase;
+          float2 v[4][3];
 #pragma unroll
-          for (int c = 0; c < 3; ++c) v[r][c] = F[r * BP + c];
-          rc[r] = vadd(v[r][0], v[r][2]);
-        }
-        float2 lm[SP];
+          for (int r = 0; r < 4; ++r)
 #pragma unroll
-        for (int k = 0; k < SP; ++k) {
-          const float2 ce = v[k + 1][1];
-          const float2 dg = vadd(rc[k], rc[k + 2]);
-          const float2 ed = vadd(vadd(v[k][1], v[k + 2][1]), rc[k + 1]);
-          const float2 four_c = vmul(four, ce);
-          const float2 G = vfma(vsplat(sk.l12, float2()), vsub(dg, four_c), vmul(vsplat(sk.lz, float2()), ce));
-          const float2 H = vfma(vsplat(sk.l23, float2()), vsub(ed, four_c), vmul(vsplat(-2.f * sk.lz, float2()), ce));
-          lm[k] = vadd(cv[k], G);
-          cv[k] = vadd(cv[SP + k], H);
-          cv[SP + k] = G;
-        }
-        if (i >= 4) {
+            for (int c = 0; c < 3; ++c) v[r][c] = F[r * BP + c];
 #pragma unroll
-          for (int k = 0; k < SP; ++k) {
-            const int c = (py0 + k) * CP + px, oa = srow(py0 + k + 2) + (px + 4);
-            const size_t g = (size_t)zc * NN + (size_t)(y0 + py0 + k) * N + (x0 + px);
-            if (grp == 0) {
-              const float2 q1 = pq[1 * CNP + c], q2 = pq[2 * CNP + c];
-              // P*_x = P_x + dt (pointwise part + eta L mu_x) (:623-629, :486-488)
-              const float psx = put_comp(oPs[0], oSlo[3], g, ac[AFP + oa], p.dt * fmaf(p.eta, lm[k].y, q2.x), zero_lo, 2);
-              amp = fmaxf(amp, fabsf(psx));
-              // phi' = phi + dt (-u.D phi + gamma L mu_0) (:631, :515), compensated: the part of
-              // the increment that rounding drops from phi is carried to the next step (otherwise
-              // increments below half an ulp of phi are lost, a systematic mass drift)
-              const float ph = ac[oa];
-              const float inc = fmaf(p.dt, fmaf(p.gamma, lm[k].x, q1.y), __uint_as_float(pre[k]));
-              const float nv = ph + inc;
-              phic[g] = inc - (nv - ph);
-              ophi[g] = nv;
-            } else {
-              const float2 q2 = pq[2 * CNP + c], q3 = pq[3 * CNP + c];
-              // P*_b = P_b + dt (pointwise part + eta L mu_b), b = y, z
-              const float2 dp2 = vmul(vsplat(p.dt, float2()), vfma(vsplat(p.eta, float2()), lm[k], f2(q2.y, q3.x)));
-              const float psy = put_comp(oPs[1], oSlo[4], g, ac[2 * AFP + oa], dp2.x, zero_lo, 2);
-              const float psz = put_comp(oPs[2], oSlo[5], g, ac[3 * AFP + oa], dp2.y, zero_lo, 2);
-              amp = fmaxf(amp, fmaxf(fabsf(psy), fabsf(psz)));
-            }
+          for (int k = 0; k < 2; ++k) {
+            // shift-invariant in-plane sums (see SepK): an off-centre plane adds
+            // G = l12 (4 diagonals - 4 centre) + lz centre, the centre plane
+            // H = l23 (4 edges - 4 centre) - 2 lz centre; G + H + G = L, zero for a constant field
+            const float2 ce = v[k + 1][1];
+            const float2 dg = vadd(vadd(v[k][0], v[k][2]), vadd(v[k + 2][0], v[k + 2][2]));
+            const float2 ed = vadd(vadd(v[k][1], v[k + 2][1]), vadd(v[k + 1][0], v[k + 1][2]));
+            const float2 four_c = vmul(four, ce);
+            const float2 G = vfma(vsplat(sk.l12, float2()), vsub(dg, four_c), vmul(vsplat(sk.lz, float2()), ce));
+            const float2 H = vfma(vsplat(sk.l23, float2()), vsub(ed, four_c), vmul(vsplat(-2.f * sk.lz, float2()), ce));
+            lm[k][q] = vadd(cv2[k * 2 + q], G);
+            cv2[k * 2 + q] = vadd(cv2[4 + k * 2 + q], H);
+            cv2[4 + k * 2 + q] = G;
           }
         }
-      } else if (grp == 2) {
         // divergence column x: X of S_xx (T3.x), Y of S_yx (T3.y), Z of S_zx
-        const float2* T = sPr + PT3 * BNP + pbase;
-        const float* Zs = sSzx + pbase;
-        float xd[SP + 2], z[SP + 2][3];
-        float2 t[SP + 2][3];
+        float dvx[2];
+        {
+          const float2* T = sPr + PT3 * BNP + pbase;
+          const float* Zs = sSzx + pbase;
+          float2 t[4][3];
+          float z[4][3];
 #pragma unroll
-        for (int r = 0; r < SP + 2; ++r) {
+          for (int r = 0; r < 4; ++r)
 #pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            t[r][c] = T[r * BP + c];
-            z[r][c] = Zs[r * BP + c];
+            for (int c = 0; c < 3; ++c) {
+              t[r][c] = T[r * BP + c];
+              z[r][c] = Zs[r * BP + c];
+            }
+#pragma unroll
+          for (int k = 0; k < 2; ++k) {
+            // differences first, then the weighted sum of the (small) differences
+            const float xd0 = t[k][2].x - t[k][0].x, xd1 = t[k + 1][2].x - t[k + 1][0].x, xd2 = t[k + 2][2].x - t[k + 2][0].x;
+            const float xr = fmaf(4.f, xd1, xd0 + xd2);
+            const float yr = fmaf(4.f, t[k + 2][1].y - t[k][1].y,
+                                  (t[k + 2][0].y - t[k][0].y) + (t[k + 2][2].y - t[k][2].y));
+            const float z0c = fmaf(4.f, z[k + 1][0], z[k][0] + z[k + 2][0]);
+            const float z1c = fmaf(4.f, z[k + 1][1], z[k][1] + z[k + 2][1]);
+            const float z2c = fmaf(4.f, z[k + 1][2], z[k][2] + z[k + 2][2]);
+            const float zr = fmaf(4.f, z1c, z0c + z2c);
+            const float Qx = xr + yr;
+            dvx[k] = cv1[k] + Qx + zr;
+            cv1[k] = fmaf(4.f, Qx, cv1[2 + k]);
+            cv1[2 + k] = Qx - zr;
           }
-          xd[r] = t[r][2].x - t[r][0].x;  // differences first, then the weighted sums
-        }
-        float dvx[SP];
-#pragma unroll
-        for (int k = 0; k < SP; ++k) {
-          const float xr = fmaf(4.f, xd[k + 1], xd[k] + xd[k + 2]);
-          const float yr = fmaf(4.f, t[k + 2][1].y - t[k][1].y, (t[k + 2][0].y - t[k][0].y) + (t[k + 2][2].y - t[k][2].y));
-          float zc3[3];
-#pragma unroll
-          for (int c = 0; c < 3; ++c) zc3[c] = fmaf(4.f, z[k + 1][c], z[k][c] + z[k + 2][c]);
-          const float zr = fmaf(4.f, zc3[1], zc3[0] + zc3[2]);
-          const float Qx = xr + yr;
-          dvx[k] = cv[k].x + Qx + zr;
-          cv[k].x = fmaf(4.f, Qx, cv[k].y);
-          cv[k].y = Qx - zr;
         }
         if (i >= 4) {
 #pragma unroll
-          for (int k = 0; k < SP; ++k) {
-            const int c = (py0 + k) * CP + px, ou = srow(py0 + k + 1) + (px + 4);
+          for (int k = 0; k < 2; ++k) {
+            const int c = (py0 + k) * CP + px, oa = srow(py0 + k + 2) + (px + 4), ou = srow(py0 + k + 1) + (px + 4);
             const size_t g = (size_t)zc * NN + (size_t)(y0 + py0 + k) * N + (x0 + px);
+            const float2 q0 = pq[0 * CNP + c], q1 = pq[1 * CNP + c], q2 = pq[2 * CNP + c], q3 = pq[3 * CNP + c];
+            const float2 A0 = f2(ac[oa], ac[AFP + oa]), A1 = f2(ac[2 * AFP + oa], ac[3 * AFP + oa]);
             // u*_x = u_x + dt d/dt u_x (:480-482)
-            const float usx = put_comp(oUs[0], oSlo[0], g, uc[ou], p.dt * fmaf(sk.d, dvx[k], pq[c].x),
-                                       __ushort_as_bfloat16((unsigned short)pre[k]), 2);
+            const float usx = put_comp(oUs[0], oSlo[0], g, uc[ou], p.dt * fmaf(sk.d, dvx[k], q0.x),
+                                       lprev[k][0], 2);
+            // P*_b = P_b + dt (pointwise part + eta L mu_b) (:623-629, :486-488)
+            const float psx = put_comp(oPs[0], oSlo[3], g, A0.y, p.dt * fmaf(p.eta, lm[k][0].y, q2.x), lprev[k][1], 2);
+            const float2 dp2 = vmul(vsplat(p.dt, float2()), vfma(vsplat(p.eta, float2()), lm[k][1], f2(q2.y, q3.x)));
+            const float psy = put_comp(oPs[1], oSlo[4], g, A1.x, dp2.x, lprev[k][2], 2);
+            const float psz = put_comp(oPs[2], oSlo[5], g, A1.y, dp2.y, lprev[k][3], 2);
             amu = fmaxf(amu, fabsf(usx));
+            amp = fmaxf(amp, fmaxf(fabsf(psx), fmaxf(fabsf(psy), fabsf(psz))));
+            // phi' = phi + dt (-u.D phi + gamma L mu_0) (:631, :515), compensated: the part of
+            // the increment that rounding drops from phi is carried to the next step (otherwise
+            // increments below half an ulp of phi are lost, a systematic mass drift)
+            const float ph = A0.x;
+            const float inc = fmaf(p.dt, fmaf(p.gamma, lm[k][0].x, q1.y), cprev[k]);
+            const float nv = ph + inc;
+            phic[g] = inc - (nv - ph);
+            ophi[g] = nv;
           }
         }
       } else {
         // divergence columns (y, z), packed: X of T0 = (S_xy, S_xz), Y of T1 = (S_yy, S_yz),
         // Z of T2 = (S_zy, S_zz)
-        const float2* X = sPr + PT0 * BNP + pbase;
-        const float2* Y = sPr + PT1 * BNP + pbase;
-        const float2* Z = sPr + PT2 * BNP + pbase;
-        float2 xr[SP], yr[SP], zr[SP];
+        float2 dv[2];
         {
-          float2 xd[SP + 2];
+          const float2* X = sPr + PT0 * BNP + pbase;
+          const float2* Y = sPr + PT1 * BNP + pbase;
+          const float2* Z = sPr + PT2 * BNP + pbase;
+          float2 xa[4][2], ya[4][3], za[4][3];
 #pragma unroll
-          for (int r = 0; r < SP + 2; ++r) xd[r] = vsub(X[r * BP + 2], X[r * BP]);  // differences first
+          for (int r = 0; r < 4; ++r) {
+            xa[r][0] = X[r * BP];
+            xa[r][1] = X[r * BP + 2];
 #pragma unroll
-          for (int k = 0; k < SP; ++k) xr[k] = vfma(four, xd[k + 1], vadd(xd[k], xd[k + 2]));
-        }
-        {
-          float2 ya[SP + 2][3];
+            for (int c = 0; c < 3; ++c) {
+              ya[r][c] = Y[r * BP + c];
+              za[r][c] = Z[r * BP + c];
+            }
+          }
 #pragma unroll
-          for (int r = 0; r < SP + 2; ++r)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) ya[r][c] = Y[r * BP + c];
-#pragma unroll
-          for (int k = 0; k < SP; ++k)
-            yr[k] = vfma(four, vsub(ya[k + 2][1], ya[k][1]), vadd(vsub(ya[k + 2][0], ya[k][0]), vsub(ya[k + 2][2], ya[k][2])));
-        }
-        {
-          float2 za[SP + 2][3];
-#pragma unroll
-          for (int r = 0; r < SP + 2; ++r)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) za[r][c] = Z[r * BP + c];
-#pragma unroll
-          for (int k = 0; k < SP; ++k) {
+          for (int k = 0; k < 2; ++k) {
+            // differences first, then the weighted sum of the (small) differences
+            const float2 xr = vfma(four, vsub(xa[k + 1][1], xa[k + 1][0]),
+                                   vadd(vsub(xa[k][1], xa[k][0]), vsub(xa[k + 2][1], xa[k + 2][0])));
+            const float2 yr = vfma(four, vsub(ya[k + 2][1], ya[k][1]),
+                                   vadd(vsub(ya[k + 2][0], ya[k][0]), vsub(ya[k + 2][2], ya[k][2])));
             const float2 t0 = vfma(four, za[k + 1][0], vadd(za[k][0], za[k + 2][0]));
             const float2 t1 = vfma(four, za[k + 1][1], vadd(za[k][1], za[k + 2][1]));
             const float2 t2 = vfma(four, za[k + 1][2], vadd(za[k][2], za[k + 2][2]));
-            zr[k] = vfma(four, t1, vadd(t0, t2));
+            const float2 zr = vfma(four, t1, vadd(t0, t2));
+            const float2 Q = vadd(xr, yr);
+            dv[k] = vadd(vadd(cv2[k], Q), zr);
+            cv2[k] = vfma(four, Q, cv2[2 + k]);
+            cv2[2 + k] = vsub(Q, zr);
           }
-        }
-        float2 dv[SP];
-#pragma unroll
-        for (int k = 0; k < SP; ++k) {
-          const float2 Q = vadd(xr[k], yr[k]);
-          dv[k] = vadd(vadd(cv[k], Q), zr[k]);
-          cv[k] = vfma(four, Q, cv[SP + k]);
-          cv[SP + k] = vsub(Q, zr[k]);
         }
         if (i >= 4) {
 #pragma unroll
-          for (int k = 0; k < SP; ++k) {
+          for (int k = 0; k < 2; ++k) {
             const int c = (py0 + k) * CP + px, ou = srow(py0 + k + 1) + (px + 4);
             const size_t g = (size_t)zc * NN + (size_t)(y0 + py0 + k) * N + (x0 + px);
             const float2 q0 = pq[0 * CNP + c], q1 = pq[1 * CNP + c];
             // (u*_y, u*_z) = (u_y, u_z) + dt d/dt (u_y, u_z) (:480-482)
             const float2 du = vmul(vsplat(p.dt, float2()), vfma(vsplat(sk.d, float2()), dv[k], f2(q0.y, q1.x)));
-            const float usy = put_comp(oUs[1], oSlo[1], g, uc[UFP + ou], du.x,
-                                       __ushort_as_bfloat16((unsigned short)pre[k]), 2);
-            const float usz = put_comp(oUs[2], oSlo[2], g, uc[2 * UFP + ou], du.y,
-                                       __ushort_as_bfloat16((unsigned short)pre[SP + k]), 2);
+            const float usy = put_comp(oUs[1], oSlo[1], g, uc[UFP + ou], du.x, lprev[k][0], 2);
+            const float usz = put_comp(oUs[2], oSlo[2], g, uc[2 * UFP + ou], du.y, lprev[k][1], 2);
             amu = fmaxf(amu, fmaxf(fabsf(usy), fabsf(usz)));
           }
         }
