@@ -66,7 +66,7 @@ KERNEL_WORDS = {
 # of one ncu capture of the default configuration on a 256^3 droplet (--clock-control none); a
 # launch over more sites scales with the sites (every kernel streams its planes once).
 TRAFFIC_BYTES_PER_SITE_F32 = {
-    "fused_rhs": (905.68e6 + 512.09e6) / 256 ** 3,
+    "fused_rhs": (1061.009e6 + 710.105e6) / 256 ** 3,
 }
 
 
