@@ -693,27 +693,45 @@ __device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, in
   // issue(i): plane z0 - 1 + i into slot i % DRD (an empty group past the last plane, so that
   // every iteration commits one). Chunks outside the domain come from the previous step's u*, P*
   // when the stale-halo quirk is on (the chunk grids are aligned with 0 and N).
+  // This thread's chunk items t = tid + k NTV (pair chunks first, then compensation chunks), the
+  // same in every plane: the wrapped offset within a plane and the staged index, with flags for
+  // a compensation chunk and for a chunk outside [0, N)^2 in (x, y). Computed once per segment.
+  constexpr int CP2 = SWP / 2, CL4 = SWL / 4;  // chunks per row
+  constexpr int NCH = SHD * (CP2 + CL4), KD = (NCH + NTV - 1) / NTV;
+  constexpr int F_LO = 1 << 30, F_OUT = 1 << 29, F_IDX = (1 << 29) - 1;
+  int goff[KD], sitem[KD];
+#pragma unroll
+  for (int k = 0; k < KD; ++k) {
+    const int t = tid + k * NTV;
+    const bool lo = t >= SHD * CP2;
+    const int tt = lo ? t - SHD * CP2 : t, cr = lo ? CL4 : CP2;
+    const int ry = tt / cr, rc = tt - ry * cr;
+    const int gx = lo ? x0 - 4 + 4 * rc : x0 - 2 + 2 * rc, gy = y0 - 1 + ry;
+    goff[k] = wrapN(gy, N) * N + wrapN(gx, N);
+    sitem[k] = t >= NCH ? -1
+                        : ((lo ? ry * SWL + 4 * rc : ry * SWP + 2 * rc) | (lo ? F_LO : 0) |
+                           ((gx < 0 || gx >= N || gy < 0 || gy >= N) ? F_OUT : 0));
+  }
   auto issue = [&](int i) {
     if (i >= niter) { cp_async_commit(); return; }
     const int zu = z0 - 1 + i;
     const bool zw = zu < 0 || zu >= N;
-    const int zz = wrapN(zu, N);
+    const size_t zo = (size_t)wrapN(zu, N) * NN;
     float2* dp = slot_p(i);
     __nv_bfloat162* dl = slot_l(i);
-    constexpr int CP2 = SWP / 2, CL4 = SWL / 4;  // chunks per row
-    for (int t = tid; t < SHD * (CP2 + CL4); t += NTV) {
-      const bool lo = t >= SHD * CP2;
-      const int tt = lo ? t - SHD * CP2 : t, cr = lo ? CL4 : CP2;
-      const int ry = tt / cr, rc = tt - ry * cr;
-      const int gx = lo ? x0 - 4 + 4 * rc : x0 - 2 + 2 * rc, gy = y0 - 1 + ry;
-      const int q = (stale_q2 && (zw || gx < 0 || gx >= N || gy < 0 || gy >= N)) ? par : par ^ 1;
-      const size_t g = (size_t)zz * NN + (size_t)wrapN(gy, N) * N + wrapN(gx, N);
-      if (lo) {
 #pragma unroll
-        for (int f = 0; f < 3; ++f) cp_async16(dl + f * SPLL + ry * SWL + 4 * rc, I.starlo[q][f] + g);
+    for (int k = 0; k < KD; ++k) {
+      const int s = sitem[k];
+      if (s < 0) continue;
+      const int q = (stale_q2 && (zw || (s & F_OUT))) ? par : par ^ 1;
+      const size_t g = zo + goff[k];
+      const int d = s & F_IDX;
+      if (s & F_LO) {
+#pragma unroll
+        for (int f = 0; f < 3; ++f) cp_async16(dl + f * SPLL + d, I.starlo[q][f] + g);
       } else {
 #pragma unroll
-        for (int f = 0; f < 3; ++f) cp_async16(dp + f * SPLP + ry * SWP + 2 * rc, I.star[q][f] + g);
+        for (int f = 0; f < 3; ++f) cp_async16(dp + f * SPLP + d, I.star[q][f] + g);
       }
     }
     cp_async_commit();
@@ -722,12 +740,6 @@ __device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, in
   const size_t gc0 = (size_t)(y0 + qy0) * N + (x0 + qx);
   const int wbp = qy0 * SWP + (qx + 1);  // staged pair index of window row 0, column x - 1
   const int wbl = qy0 * SWL + (qx + 3);  // the same in the compensation rows
-  // column x sits at staged index qx + 2 (pairs) and qx + 4 (compensations), both even when qx is:
-  // the aligned two-column load that holds it starts at window column pb (1 for even qx, else 0)
-  // and the third column of the window is sc
-  const bool odd = (qx & 1) != 0;
-  const int pb = odd ? 0 : 1, sc = odd ? 2 : 0;
-  static_assert(SWP % 2 == 0 && SPLP % 2 == 0 && SWL % 2 == 0 && SPLL % 2 == 0, "aligned column pairs");
   // the divergence D_x v_x + D_y v_y + D_z v_z of v = (u*, P*) (getStream mode 0, :664-670), each
   // D = d/36 delta s s: a plane adds Q = delta_x s_y v_x + s_x delta_y v_y with weight s_z =
   // (1, 4, 1) and Z = s_x s_y v_z with weight delta_z = (-1, 0, 1) over planes c-1, c, c+1.
@@ -753,21 +765,14 @@ __device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, in
     issue(i + DRD - 1);  // into the slot read at iteration i - 1
     const float2* sp = slot_p(i) + wbp;
     const __nv_bfloat162* sl = slot_l(i) + wbl;
-    // the three columns x - 1, x, x + 1 of component f in window row r, split: the aligned
-    // two-column loads that hold x and the remaining column
+    // the three columns x - 1, x, x + 1 of component f in window row r, split (one 8-byte load
+    // per column of the pairs and one 4-byte load of the compensations: the same shared-memory
+    // wavefronts as wider aligned loads, without lane-dependent selects)
     auto row3 = [&](int f, int r, float2* q, float2* rest) {
       const float2* a = sp + f * SPLP + r * SWP;
       const __nv_bfloat162* b = sl + f * SPLL + r * SWL;
-      const float4 pr = *reinterpret_cast<const float4*>(a + pb);
-      const float2 sv = a[sc];
-      const uint2 lr = *reinterpret_cast<const uint2*>(b + pb);
-      const __nv_bfloat162 lv = b[sc];
-      const float2 p0 = f2(pr.x, pr.y), p1 = f2(pr.z, pr.w);
-      const __nv_bfloat162 l0 = *reinterpret_cast<const __nv_bfloat162*>(&lr.x);
-      const __nv_bfloat162 l1 = *reinterpret_cast<const __nv_bfloat162*>(&lr.y);
-      split(odd ? p0 : sv, odd ? l0 : lv, q[0], rest[0]);
-      split(odd ? p1 : p0, odd ? l1 : l0, q[1], rest[1]);
-      split(odd ? sv : p1, odd ? lv : l1, q[2], rest[2]);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) split(a[c], b[c], q[c], rest[c]);
     };
     // per row of the window and part: the x-part delta_x v_x, and s_x of v_y and of v_z
     float2 xd[2][USD + 2], ys[2][USD + 2], zs[2][USD + 2];
