@@ -795,8 +795,7 @@ void append_cache(const char* path, const std::string& key, const ttsh_tuning& t
 // Whether kernels may read and write the host range [p, p + bytes) in place: it is page-locked
 // (cudaHostAlloc / cudaHostRegister; in the unified address space its host address is also its
 // device address), checked at both ends. Pageable arrays are staged by the copy engines.
-static bool host_direct(ttsh_sim* s, const void* p, size_t bytes) {
-  (void)s;
+static bool host_direct(const void* p, size_t bytes) {
   if (!p || !bytes) return false;
   const char* c = static_cast<const char*>(p);
   for (const char* q : {c, c + bytes - 1}) {
@@ -822,7 +821,7 @@ static void h2d(ttsh_sim* s, T* dst, const double* src, size_t n, double* scratc
   if constexpr (sizeof(T) == sizeof(double)) {
     CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, st));
   } else {
-    if (!host_direct(s, src, n * sizeof(double))) {
+    if (!host_direct(src, n * sizeof(double))) {
       CK(cudaMemcpyAsync(scratch, src, n * sizeof(double), cudaMemcpyHostToDevice, st));
       src = scratch;
     }
@@ -833,7 +832,7 @@ template <class T>
 static void d2h(ttsh_sim* s, double* dst, const T* src, size_t n, double* scratch, size_t stride = 1,
                 const int* scale_bits = nullptr) {
   const cudaStream_t st = s->stream;
-  const bool direct = host_direct(s, dst, n * sizeof(double));
+  const bool direct = host_direct(dst, n * sizeof(double));
   if constexpr (sizeof(T) == sizeof(double)) {
     if (stride == 1) CK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, st));
     else if (direct) launch_gather_f64(src, stride, dst, n, st);
@@ -1026,7 +1025,7 @@ int ttsh_set_state(ttsh_sim* s, int inst, const double* phi, const double* P, co
       double* scr = conv_scratch(s, I);
       // the split kernel reads the host array in place when it can (host_direct), else a staged copy
       auto stage = [&](const double* src) -> const double* {
-        if (host_direct(s, src, n * sizeof(double))) return src;
+        if (host_direct(src, n * sizeof(double))) return src;
         CK(cudaMemcpyAsync(scr, src, n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
         return scr;
       };
@@ -1112,7 +1111,7 @@ int ttsh_get_state(ttsh_sim* s, int inst, double* phi, double* P, double* u, dou
       if constexpr (std::is_same<TT, float>::value) {
         if (s->fused) {  // the compensated values
           auto get = [&](double* dst, const float* hi, const __nv_bfloat16* lo, const float* lo32) {
-            if (host_direct(s, dst, n * sizeof(double))) {  // joined straight into the host array
+            if (host_direct(dst, n * sizeof(double))) {  // joined straight into the host array
               launch_join(hi, lo, lo32, dst, n, 1, s->stream);
               return;
             }
@@ -1163,7 +1162,7 @@ int ttsh_get_provisional(ttsh_sim* s, int inst, double* ustar, double* Pstar) {
             const float* sh = reinterpret_cast<const float*>(I.star[s->par][b]);
             const __nv_bfloat16* sl = reinterpret_cast<const __nv_bfloat16*>(I.starlo[s->par][b]);
             auto get2 = [&](double* dst, const float* hi, const __nv_bfloat16* lo) {  // one half of the pairs
-              if (host_direct(s, dst, n * sizeof(double))) {
+              if (host_direct(dst, n * sizeof(double))) {
                 launch_join(hi, lo, nullptr, dst, n, 2, s->stream);
                 return;
               }
