@@ -652,8 +652,11 @@ constexpr size_t DIV_SLOT = 3 * SPLP * sizeof(float2) + 3 * SPLL * sizeof(__nv_b
 constexpr size_t DIV_SMEM = DRD * DIV_SLOT;
 static_assert((3 * SPLP * sizeof(float2)) % 16 == 0 && DIV_SLOT % 16 == 0, "16-byte aligned staging");
 static_assert(2 * DIV_SMEM <= 227 * 1024, "fused_div: two CTAs per SM");
-constexpr size_t COR_SLOT = CPL * sizeof(float2) + 3 * CN * sizeof(float2);  // p_v, p_p on B; (u*, P*) pairs on C
+// p_v, p_p on B; the (u*, P*) pairs and their bf16x2 compensations on C
+constexpr size_t COR_SLOT = CPL * sizeof(float2) + 3 * CN * sizeof(float2) + 3 * CN * sizeof(__nv_bfloat162);
+static_assert(COR_SLOT % 16 == 0 && (CPL * sizeof(float2)) % 16 == 0, "16-byte aligned ring slots");
 constexpr size_t COR_SMEM = DR * COR_SLOT;
+static_assert(2 * COR_SMEM <= 227 * 1024, "fused_correct: two CTAs per SM");
 
 // wait until at most DR - 2 copy groups are pending: the group of the plane read now is complete
 __device__ __forceinline__ void cp_async_wait_ring() {
@@ -839,8 +842,12 @@ __device__ __forceinline__ void correct_segment(const InstDev<float>& I, int par
   const int tid = threadIdx.x;
   auto slot_w = [&](int i) { return reinterpret_cast<float2*>(smc + (i % DR) * COR_SLOT); };
   auto slot_q = [&](int i) { return reinterpret_cast<float2*>(smc + (i % DR) * COR_SLOT + CPL * sizeof(float2)); };
+  auto slot_l = [&](int i) {
+    return reinterpret_cast<__nv_bfloat162*>(smc + (i % DR) * COR_SLOT + CPL * sizeof(float2) + 3 * CN * sizeof(float2));
+  };
   // issue(i): into slot i % DR the pressures (p_v, p_p) of plane z0 - 1 + i over tile+1 and u*, P*
-  // of plane z0 - 2 + i (finished at iteration i) over the tile; an empty group past the last plane
+  // of plane z0 - 2 + i (finished at iteration i) with their compensations over the tile; an empty
+  // group past the last plane
   auto issue = [&](int i) {
     if (i >= niter) { cp_async_commit(); return; }
     const int zz = wrapN(z0 - 1 + i, N);
@@ -861,6 +868,15 @@ __device__ __forceinline__ void correct_segment(const InstDev<float>& I, int par
         const int ry = r / QR, rc = r - ry * QR;
         cp_async16(dq + f * CN + ry * TX + 2 * rc, I.star[par ^ 1][f] + (size_t)zq * NN + (size_t)(y0 + ry) * N + x0 + 2 * rc);
       }
+      // their compensations: 16-byte chunks of 4 sites
+      __nv_bfloat162* dl = slot_l(i);
+      constexpr int LR = TX / 4, LF = TY * LR;  // chunks per tile row, per field
+      for (int t = tid; t < 3 * LF; t += NTC) {
+        const int f = t / LF, r = t - f * LF;
+        const int ry = r / LR, rc = r - ry * LR;
+        cp_async16(dl + f * CN + ry * TX + 4 * rc,
+                   I.starlo[par ^ 1][f] + (size_t)zq * NN + (size_t)(y0 + ry) * N + x0 + 4 * rc);
+      }
     }
     cp_async_commit();
   };
@@ -872,13 +888,6 @@ __device__ __forceinline__ void correct_segment(const InstDev<float>& I, int par
 #pragma unroll
   for (int k = 0; k < DR - 1; ++k) issue(k);
   for (int i = 0; i < niter; ++i) {
-    // the compensations of (u*_b, P*_b) at this iteration's output site, loaded before the wait
-    __nv_bfloat162 sl[3];
-    if (i >= 2) {
-      const size_t g = (size_t)(z0 - 2 + i) * NN + gc;
-#pragma unroll
-      for (int f = 0; f < 3; ++f) sl[f] = I.starlo[par ^ 1][f][g];
-    }
     cp_async_wait_ring();
     __syncthreads();
     issue(i + DR - 1);  // into the slot read at iteration i - 1
@@ -908,6 +917,7 @@ __device__ __forceinline__ void correct_segment(const InstDev<float>& I, int par
       // getVNew (TTSH3D.cu:505-511): u = u* - dt D p_v, P = P* - dt D p_p
       const size_t g = (size_t)(z0 - 2 + i) * NN + gc;
       const float2* qc = slot_q(i) + qy * TX + qx;
+      const __nv_bfloat162* lc = slot_l(i) + qy * TX + qx;
       const float gv[3] = {gx.x, gy.x, gz.x}, gp[3] = {gx.y, gy.y, gz.y};
       // u compensated: the FP32 value and, in bf16, what its rounding dropped plus u*'s
       // compensation. P: the FP32 value nearest the exact P* - dt D p_p (its compensation is not
@@ -917,10 +927,11 @@ __device__ __forceinline__ void correct_segment(const InstDev<float>& I, int par
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
         const float2 st = qc[b * CN];
-        put_comp(oU[b], I.lo[b], g, st.x, -(dt * (kd * (gv[b] * du))), __low2bfloat16(sl[b]));
+        const __nv_bfloat162 sl = lc[b * CN];
+        put_comp(oU[b], I.lo[b], g, st.x, -(dt * (kd * (gv[b] * du))), __low2bfloat16(sl));
         float e;
         const float v = two_sum(st.y, -(dt * (kd * (gp[b] * dp))), e);
-        oP[b][g] = v + (e + __bfloat162float(__high2bfloat16(sl[b])));
+        oP[b][g] = v + (e + __bfloat162float(__high2bfloat16(sl)));
       }
     }
   }
