@@ -68,6 +68,12 @@ KERNEL_WORDS = {
 TRAFFIC_BYTES_PER_SITE_F32 = {
     "fused_rhs": (1061.009e6 + 710.105e6) / 256 ** 3,
 }
+# Warp instructions per site of the dominant FP32 kernels (smsp__inst_executed.sum of the same
+# capture / sites): with the SM count, 4 schedulers per SM and the sampled SM clock they give the
+# time the kernel's instruction issue alone takes, the other bound of an on-chip-limited kernel.
+INSTR_PER_SITE_F32 = {
+    "fused_rhs": 539993606 / 256 ** 3,
+}
 
 
 def workload(name: str):
@@ -413,6 +419,12 @@ def main():
     if args.precision == 32 and dom_name in TRAFFIC_BYTES_PER_SITE_F32:
         traffic = TRAFFIC_BYTES_PER_SITE_F32[dom_name] * sites
     launches = sim.launches_per_step()
+    issue_ms = None
+    if args.precision == 32 and dom_name in INSTR_PER_SITE_F32:
+        sm_mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz")
+        if sm_mhz:
+            sms = torch.cuda.get_device_properties(local).multi_processor_count
+            issue_ms = INSTR_PER_SITE_F32[dom_name] * sites / (sms * 4 * sm_mhz * 1e6) * 1e3
 
     # end to end through the public API: host state -> device, K steps each followed by the
     # FP64 mass/divergence read-back, final state -> host
@@ -508,7 +520,11 @@ def main():
                          "traffic_source": "ncu DRAM read+write bytes of one 256^3 launch, scaled by sites"
                          if traffic is not None else None,
                          "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
-                         peak_kind, "bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms / max(1, dom_launches)},
+                         peak_kind, "bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms / max(1, dom_launches),
+                         "issue_bound_ms": issue_ms,
+                         "issue_frac": issue_ms / (dom_ms / max(1, dom_launches)) if issue_ms and dom_ms > 0 else None,
+                         "issue_source": "ncu warp instructions per site of one 256^3 launch x sites / (SMs x 4 "
+                                         "schedulers x median SM clock under load)" if issue_ms else None},
             "kernels_ms_per_step": {k: round(v[0], 4) for k, v in prof.items()},
             "gpu_launches": launches * args.steps,
             "launches_per_step": launches,
