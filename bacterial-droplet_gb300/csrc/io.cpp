@@ -2,6 +2,7 @@
 // writer and the build-defined initial condition. No CUDA here.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -14,6 +15,62 @@
 #include "internal.h"
 
 using ttsh::set_error;
+
+namespace {
+
+// printf "%.15f" of x, written at p (at least F15_MAX bytes of room); returns the end. printf
+// prints the exact binary value of x rounded to 15 decimals, ties to even. For |x| < 2^13 that
+// value is computed exactly: x = m 2^e with m < 2^53 and e <= -40, so m 10^15 < 2^103 fits
+// 128-bit integers and the rounding of m 10^15 / 2^-e is decided on the exact remainder. The sign
+// is printed whenever x's sign bit is set, as printf does for -0.0 and for negative values that
+// round to zero. Larger magnitudes, infinities and NaNs go to snprintf itself.
+constexpr int F15_MAX = 340;  // "-" + 309 integer digits + "." + 15 decimals + NUL, rounded up
+char* put_f15(char* p, double x) {
+  uint64_t bits;
+  std::memcpy(&bits, &x, sizeof bits);
+  const int be = (int)((bits >> 52) & 0x7ff);
+  if (be >= 1023 + 13) return p + std::snprintf(p, F15_MAX, "%.15f", x);  // |x| >= 2^13, inf, nan
+  constexpr uint64_t P15 = 1000000000000000ull;
+  uint64_t m = bits & ((1ull << 52) - 1);
+  int e;
+  if (be == 0) {
+    e = -1074;  // subnormal
+  } else {
+    m |= 1ull << 52;
+    e = be - 1075;  // <= -40 here
+  }
+  uint64_t r;  // |x| 10^15 rounded to an integer, ties to even (< 2^13 10^15 < 2^63)
+  if (-e >= 128) {
+    r = 0;  // |x| 10^15 < 2^103 / 2^128
+  } else {
+    const unsigned __int128 v = (unsigned __int128)m * P15;
+    const int s = -e;
+    const unsigned __int128 q = v >> s;
+    const unsigned __int128 rem = v - (q << s);
+    const unsigned __int128 half = (unsigned __int128)1 << (s - 1);
+    r = (uint64_t)q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+  }
+  if (bits >> 63) *p++ = '-';
+  const uint64_t ip = r / P15;
+  uint64_t fp = r - ip * P15;
+  // integer part (< 2^13 + 1)
+  char ib[8];
+  int ni = 0;
+  uint64_t t = ip;
+  do {
+    ib[ni++] = (char)('0' + t % 10);
+    t /= 10;
+  } while (t);
+  while (ni) *p++ = ib[--ni];
+  *p++ = '.';
+  for (int k = 14; k >= 0; --k) {
+    p[k] = (char)('0' + fp % 10);
+    fp /= 10;
+  }
+  return p + 15;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -84,39 +141,56 @@ int ttsh_format_conf(int N, int expo_data, const double* phi, const double* P, c
   const size_t n = (size_t)N * N * N;
   const size_t NN = (size_t)N * N;
   unsigned nth = std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
-  // Each round formats nth chunks of consecutive y-planes (the outer loop) and writes them in
-  // order; a chunk holds about 8 MB of text at most, so memory stays bounded.
+  // Each round formats nth chunks of consecutive y-planes (the outer loop); a chunk holds about 8 MB
+  // of text at most, so memory stays bounded (two rounds). A writer thread writes round k in order
+  // while round k + 1 is formatted.
   const int chunk_rows = std::max(1, (int)std::min<size_t>((size_t)N / nth, (size_t)(8u << 20) / (NN * 140)));
   int err = 0;
-  for (int y0 = 0; y0 < N && !err; y0 += chunk_rows * (int)nth) {
-    std::vector<std::string> bufs(nth);
+  std::vector<std::string> bufs[2] = {std::vector<std::string>(nth), std::vector<std::string>(nth)};
+  std::thread writer;
+  int round = 0;
+  for (int y0 = 0; y0 < N; y0 += chunk_rows * (int)nth, ++round) {
+    std::vector<std::string>& cur = bufs[round & 1];
     std::vector<std::thread> th;
     for (unsigned t = 0; t < nth; ++t) {
       th.emplace_back([&, t]() {
         const int ya = y0 + (int)t * chunk_rows;
         const int yb = std::min(N, ya + chunk_rows);
+        std::string& out = cur[t];
+        out.clear();
         if (ya >= yb) return;
-        std::string& out = bufs[t];
         out.reserve((size_t)(yb - ya) * NN * (expo_data == 1 ? 7 * 20 : 2 * 20));
-        char tmp[512];
+        char tmp[7 * (F15_MAX + 1)];  // 7 values and their separators
         for (int y = ya; y < yb; ++y)
           for (int x = 0; x < N; ++x)
             for (int z = 0; z < N; ++z) {
               const size_t i = ((size_t)z * N + y) * N + x;
-              int len;
-              if (expo_data == 1)
-                len = std::snprintf(tmp, sizeof(tmp), "%.15f %.15f %.15f %.15f %.15f %.15f %.15f\n", u[i], u[n + i],
-                                    u[2 * n + i], P[i], P[n + i], P[2 * n + i], phi[i]);
-              else
-                len = std::snprintf(tmp, sizeof(tmp), "%.15f %.15f ", u[i], u[n + i]);
-              out.append(tmp, (size_t)len);
+              char* q = tmp;
+              if (expo_data == 1) {
+                const double v[7] = {u[i], u[n + i], u[2 * n + i], P[i], P[n + i], P[2 * n + i], phi[i]};
+                for (int c = 0; c < 7; ++c) {
+                  q = put_f15(q, v[c]);
+                  *q++ = c < 6 ? ' ' : '\n';
+                }
+              } else {
+                q = put_f15(q, u[i]);
+                *q++ = ' ';
+                q = put_f15(q, u[n + i]);
+                *q++ = ' ';
+              }
+              out.append(tmp, (size_t)(q - tmp));
             }
       });
     }
     for (auto& t : th) t.join();
-    for (auto& b : bufs)
-      if (!b.empty() && std::fwrite(b.data(), 1, b.size(), fp) != b.size()) err = 1;
+    if (writer.joinable()) writer.join();  // round k - 1 written: its buffers may be reused next
+    std::vector<std::string>* done = &cur;
+    writer = std::thread([done, fp, &err]() {
+      for (auto& b : *done)
+        if (!b.empty() && std::fwrite(b.data(), 1, b.size(), fp) != b.size()) err = 1;
+    });
   }
+  if (writer.joinable()) writer.join();
   if (std::fclose(fp) != 0) err = 1;
   if (err) return set_error(TTSH_E_IO, std::string("write failed: ") + path);
   return TTSH_OK;

@@ -298,12 +298,15 @@ def run_snapshot(args):
                        "steps_after_async_s": t5 - t3, "async_total_s": t6 - t3, "async_bytes": nbytes_async,
                        "exposed_s": (t6 - t3) - (t3 - t2),
                        "form": "FP32 fused, 1 droplet, cores %d" % (os.cpu_count() or 0)}
-        try:
-            import make_ref
-            binary = make_ref.build()
-        except Exception as e:
-            binary = None
-            out["reference"] = {"unavailable": "reference program not built: %s" % str(e)[:200]}
+        binary = None
+        if args.snapshot_skip_reference:
+            out["reference"] = {"skipped": "--snapshot-skip-reference"}
+        else:
+            try:
+                import make_ref
+                binary = make_ref.build()
+            except Exception as e:
+                out["reference"] = {"unavailable": "reference program not built: %s" % str(e)[:200]}
         if binary:
             import make_ref_golden as G
             import oracle
@@ -349,6 +352,8 @@ def main():
     ap.add_argument("--snapshot", action="store_true",
                     help="measure the snapshot writer (text bytes/s) against the reference's ExpoConf and exit")
     ap.add_argument("--snapshot-n", type=int, default=256)
+    ap.add_argument("--snapshot-skip-reference", action="store_true",
+                    help="with --snapshot: time only this library's writer")
     args = ap.parse_args()
     if args.snapshot:
         run_snapshot(args)

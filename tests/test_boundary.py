@@ -237,3 +237,47 @@ def test_reference_input_text_is_the_writer_output(tmp_path):
         p = tmp_path / ("in_%d.dat" % N)
         ttsh.write_input(str(p), ttsh.default_input(Nx=N, Ny=N, Nz=N, Ts=Ts, dte=dte, ExpoData=expo))
         assert G.reference_input_text(N, Ts, dte, expo) == p.read_text(), N
+
+
+def test_snapshot_number_format_on_hard_values(tmp_path):
+    """The snapshot writer prints every value exactly as printf "%.15f" does (the reference's
+    `fixed << setprecision(15)`): its exact binary value rounded to 15 decimals with ties to even,
+    the sign of -0.0 and of negatives that round to zero kept. Checked against Python's correctly
+    rounded formatting on exact ties (odd multiples of 2^-16, whose 16th decimal is a final 5),
+    values next to the 2^13 bound of the integer path and beyond it, subnormals and random values
+    over many magnitudes."""
+    import numpy as np
+    import ttsh
+    rng = np.random.default_rng(5)
+    special = [0.0, -0.0, 1.0, -1.0, 0.5, 1 / 65536, 3 / 65536, -5 / 65536, 2 ** -17, 7 * 2 ** -18,
+               1e-15, 5e-16, -5e-16, 4.9999999999999996e-16, -1e-17, 1e-300, -1e-300, 5e-324, -5e-324,
+               2.2250738585072014e-308, 8191.999999999999, 8191.9999999999995, 8192.0, -8192.0, 8192.5,
+               12345.678901234567, -1e10, 1.7976931348623157e308, 0.1, 0.2, 0.3, 2 / 3, -2 / 3,
+               1 - 2 ** -53, 1 + 2 ** -52, 999.9999999999995, 0.0000000000000015, 0.0000000000000025]
+    ties = list((2 * rng.integers(0, 2 ** 20, 200) + 1) / 65536.0 * rng.choice([-1, 1], 200))
+    mags = list(rng.standard_normal(2000) * 10.0 ** rng.integers(-18, 4, 2000))
+    vals = np.array(special + ties + mags, dtype=np.float64)
+    N = 8
+    n = N ** 3
+    buf = np.resize(vals, 7 * n)
+    u = buf[:3 * n].reshape(3, N, N, N).copy()
+    P = buf[3 * n:6 * n].reshape(3, N, N, N).copy()
+    phi = buf[6 * n:].reshape(N, N, N).copy()
+    path = str(tmp_path / "conf_1.dat")
+    ttsh.format_conf(path, phi, P, u)
+    lines = open(path).read().split("\n")
+    assert len(lines) == n + 1 and lines[-1] == ""
+    k = 0
+    for y in range(N):
+        for x in range(N):
+            for z in range(N):
+                vs = [u[0, z, y, x], u[1, z, y, x], u[2, z, y, x], P[0, z, y, x], P[1, z, y, x],
+                      P[2, z, y, x], phi[z, y, x]]
+                assert lines[k] == " ".join("%.15f" % v for v in vs), (k, lines[k])
+                k += 1
+    # the 2-column layout (ExpoData == -1): "vx vy " per site, no newline
+    path2 = str(tmp_path / "conf_2.dat")
+    ttsh.format_conf(path2, phi, P, u, expo_data=-1)
+    exp = "".join("%.15f %.15f " % (u[0, z, y, x], u[1, z, y, x])
+                  for y in range(N) for x in range(N) for z in range(N))
+    assert open(path2).read() == exp
