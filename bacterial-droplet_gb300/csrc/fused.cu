@@ -27,10 +27,11 @@
 // carries the z-combination in registers from plane to plane, so every product plane is read
 // once.
 //
-// fused_rhs keeps its fields in pairs, interleaved in shared memory as float2 ((phi, Px),
-// (Py, Pz), (ux, uy), and pairs of products): one 64-bit load fetches both, and the stencil
-// arithmetic runs on both with the packed FP32 instructions of sm_100+ (add/mul/fma .f32x2, two
-// independent IEEE FP32 operations with round-to-nearest, the same results as two scalar ones).
+// fused_rhs computes on pairs of fields ((phi, Px), (Py, Pz), (ux, uy), and pairs of products)
+// with the packed FP32 instructions of sm_100+ (add/mul/fma .f32x2, two independent IEEE FP32
+// operations with round-to-nearest, the same results as two scalar ones). The state planes are
+// staged planar (one array per field, 16-byte copies); the products are stored as float2 pairs,
+// so that one 64-bit load fetches both.
 //
 // The stencil arithmetic is the reference's 27-point and 15-point weights (st_dx/st_dy/st_dz/
 // st_lap of common.cuh, TTSH3D.cu:3280-3343) in FP32, regrouped separably; the stress enters as
