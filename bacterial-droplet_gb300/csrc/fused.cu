@@ -17,7 +17,7 @@
 // whatever rounding it carries into the pressure.
 //
 // All three march along z through a tile of columns (a "2.5D" sweep; fused_rhs 32 x 8, fused_div
-// 32 x 32, fused_correct 32 x 16), on a chunked or a persistent schedule: each z-plane of
+// 32 x 16, fused_correct 32 x 16), on a chunked or a persistent schedule: each z-plane of
 // every field the stencils need is staged once in a shared-memory ring of planes, and each
 // thread evaluates the 27-point derivatives / 15-point Laplacians of a 1 x R strip of sites
 // from its 3 x (R+2) x 3 neighbourhood, so warps read shared memory with unit stride. The
@@ -643,16 +643,16 @@ constexpr int SH = TY + 2;              // staged rows y0 - 1 .. y0 + TY
 constexpr int CW = TX + 4;              // fused_correct row, float2 x0 - 2 .. x0 + TX + 1
 constexpr int CPL = CW * SH;            // float2 per staged plane
 constexpr int DR = 4;                   // ring slots of fused_correct
-// fused_div: a taller tile (TX x TYD) and a 2-slot ring (1 plane in flight); each slot holds the
-// pairs (u*_b, P*_b) (rows x0 - 2 .. x0 + TX + 1, 16-byte chunks of 2 sites) and their bf16
-// compensations (rows x0 - 4 .. x0 + TX + 3, chunks of 4 sites)
-constexpr int TYD = 32, SHD = TYD + 2, DRD = 2;
+// fused_div: TX x TYD tiles and a 3-slot ring (2 planes in flight), three CTAs per SM; each slot
+// holds the pairs (u*_b, P*_b) (rows x0 - 2 .. x0 + TX + 1, 16-byte chunks of 2 sites) and their
+// bf16 compensations (rows x0 - 4 .. x0 + TX + 3, chunks of 4 sites)
+constexpr int TYD = 16, SHD = TYD + 2, DRD = 3;
 constexpr int SWP = TX + 4, SPLP = SWP * SHD;  // float2 per row, per plane
 constexpr int SWL = TX + 8, SPLL = SWL * SHD;  // bf16x2 per row, per plane
 constexpr size_t DIV_SLOT = 3 * SPLP * sizeof(float2) + 3 * SPLL * sizeof(__nv_bfloat162);
 constexpr size_t DIV_SMEM = DRD * DIV_SLOT;
 static_assert((3 * SPLP * sizeof(float2)) % 16 == 0 && DIV_SLOT % 16 == 0, "16-byte aligned staging");
-static_assert(2 * DIV_SMEM <= 227 * 1024, "fused_div: two CTAs per SM");
+static_assert(3 * DIV_SMEM <= 227 * 1024, "fused_div: three CTAs per SM");
 // p_v, p_p on B; the (u*, P*) pairs and their bf16x2 compensations on C
 constexpr size_t COR_SLOT = CPL * sizeof(float2) + 3 * CN * sizeof(float2) + 3 * CN * sizeof(__nv_bfloat162);
 static_assert(COR_SLOT % 16 == 0 && (CPL * sizeof(float2)) % 16 == 0, "16-byte aligned ring slots");
@@ -664,10 +664,10 @@ __device__ __forceinline__ void cp_async_wait_ring() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(DR - 2) : "memory");
 }
 
-// fused_div: 4-site strips of a 32 x 32 tile (a 6 x 3 window of each staged field serves the
+// fused_div: 4-site strips of a 32 x 16 tile (a 6 x 3 window of each staged field serves the
 // four sites), u* and P* as a packed pair.
 constexpr int USD = 4;                   // sites per strip
-constexpr int NTV = TX * TYD / USD;      // 256 threads
+constexpr int NTV = TX * TYD / USD;      // 128 threads
 __device__ __forceinline__ void cp_async_wait_div() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(DRD - 2) : "memory");
 }
@@ -820,7 +820,7 @@ __device__ __forceinline__ void div_segment(const InstDev<float>& I, int par, in
 }
 
 template <bool PERSIST>
-__global__ void __launch_bounds__(NTV, 2) k_fused_div(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc,
+__global__ void __launch_bounds__(NTV, 3) k_fused_div(const InstDev<float>* __restrict__ insts, int par, int nchunk, int zc,
                                                        int ninst) {
   extern __shared__ __align__(16) unsigned char smd[];
   const int N = insts[0].N;
