@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <memory>
 #include <random>
 #include <string>
 #include <thread>
@@ -255,57 +256,84 @@ extern "C" int ttsh_init_droplet(int N, double h, double R, double xi, uint64_t 
     return set_error(TTSH_E_INVALID, "ttsh_init_droplet: bad arguments");
   const size_t n = (size_t)N * N * N;
   const double c = N / 2.0, twopi = 6.283185307179586476925286766559;
-  std::vector<double> Q(3 * n, 0.0);
-  for (int z = 0; z < N; ++z)
-    for (int y = 0; y < N; ++y)
-      for (int x = 0; x < N; ++x) {
-        const size_t i = ((size_t)z * N + y) * N + x;
-        const double dx = x - c, dy = y - c, dz = z - c;
-        const double r = h * std::sqrt(dx * dx + dy * dy + dz * dz);
-        phi[i] = 0.5 * (1.0 - std::tanh((r - R) / xi));
-        if (phi[i] > 0.5) {
-          const double cz = 1.0 - 2.0 * uni(seed, i, 0);
-          const double az = twopi * uni(seed, i, 1);
-          const double s = std::sqrt(std::max(0.0, 1.0 - cz * cz));
-          double v[3] = {s * std::cos(az), s * std::sin(az), cz};
-          if (angular_noise > 0) {
-            double g[3];
-            for (int k = 0; k < 3; ++k) {  // Box-Muller
-              const double u1 = 1.0 - uni(seed, i, 2 + k), u2 = uni(seed, i, 5 + (k % 3));
-              g[k] = std::sqrt(-2.0 * std::log(u1)) * std::cos(twopi * u2);
+  // scratch left uninitialised here: the slabs below write every element (and touch its pages) on
+  // the thread that computes it
+  std::unique_ptr<double[]> Qb(new double[3 * n]), Tb(new double[3 * n]);
+  double* Q = Qb.get();
+  double* T2 = Tb.get();
+  // Every site is a function of its own index (counter-based draws) and, in the smoothing passes,
+  // of the previous pass: z-slabs are computed on all host cores with the same results.
+  const unsigned nth = std::max(1u, std::min({64u, std::thread::hardware_concurrency(), (unsigned)N}));
+  auto slabs = [&](auto&& body) {
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nth; ++t)
+      th.emplace_back([&, t]() {
+        const int z0 = (int)((long long)N * t / nth), z1 = (int)((long long)N * (t + 1) / nth);
+        body(z0, z1);
+      });
+    for (auto& t : th) t.join();
+  };
+  slabs([&](int z0, int z1) {
+    for (int z = z0; z < z1; ++z)
+      for (int y = 0; y < N; ++y)
+        for (int x = 0; x < N; ++x) {
+          const size_t i = ((size_t)z * N + y) * N + x;
+          const double dx = x - c, dy = y - c, dz = z - c;
+          const double r = h * std::sqrt(dx * dx + dy * dy + dz * dz);
+          phi[i] = 0.5 * (1.0 - std::tanh((r - R) / xi));
+          if (phi[i] > 0.5) {
+            const double cz = 1.0 - 2.0 * uni(seed, i, 0);
+            const double az = twopi * uni(seed, i, 1);
+            const double s = std::sqrt(std::max(0.0, 1.0 - cz * cz));
+            double v[3] = {s * std::cos(az), s * std::sin(az), cz};
+            if (angular_noise > 0) {
+              double g[3];
+              for (int k = 0; k < 3; ++k) {  // Box-Muller
+                const double u1 = 1.0 - uni(seed, i, 2 + k), u2 = uni(seed, i, 5 + (k % 3));
+                g[k] = std::sqrt(-2.0 * std::log(u1)) * std::cos(twopi * u2);
+              }
+              const double gp = g[0] * v[0] + g[1] * v[1] + g[2] * v[2];
+              double w[3], nn = 0;
+              for (int k = 0; k < 3; ++k) {
+                w[k] = v[k] + angular_noise * (g[k] - gp * v[k]);
+                nn += w[k] * w[k];
+              }
+              nn = std::sqrt(nn);
+              for (int k = 0; k < 3; ++k) v[k] = w[k] / nn;
             }
-            const double gp = g[0] * v[0] + g[1] * v[1] + g[2] * v[2];
-            double w[3], nn = 0;
-            for (int k = 0; k < 3; ++k) {
-              w[k] = v[k] + angular_noise * (g[k] - gp * v[k]);
-              nn += w[k] * w[k];
-            }
-            nn = std::sqrt(nn);
-            for (int k = 0; k < 3; ++k) v[k] = w[k] / nn;
+            for (int k = 0; k < 3; ++k) Q[k * n + i] = v[k];
+          } else {
+            for (int k = 0; k < 3; ++k) Q[k * n + i] = 0.0;
           }
-          for (int k = 0; k < 3; ++k) Q[k * n + i] = v[k];
+        }
+  });
+  // 3 Jacobi passes: mean of self and the 6 face neighbours, periodic.
+  const size_t NN = (size_t)N * N;
+  for (int pass = 0; pass < 3; ++pass) {
+    slabs([&](int z0, int z1) {
+      for (int k = 0; k < 3; ++k) {
+        const double* a = &Q[k * n];
+        double* b = &T2[k * n];
+        for (int z = z0; z < z1; ++z) {
+          const size_t zm = (size_t)(z == 0 ? N - 1 : z - 1) * NN, zc = (size_t)z * NN,
+                       zp = (size_t)(z == N - 1 ? 0 : z + 1) * NN;
+          for (int y = 0; y < N; ++y) {
+            const size_t ym = (size_t)(y == 0 ? N - 1 : y - 1) * N, yc = (size_t)y * N,
+                         yp = (size_t)(y == N - 1 ? 0 : y + 1) * N;
+            for (int x = 0; x < N; ++x) {
+              const int xm = x == 0 ? N - 1 : x - 1, xp = x == N - 1 ? 0 : x + 1;
+              b[zc + yc + x] = (a[zc + yc + x] + a[zc + yc + xm] + a[zc + yc + xp] + a[zc + ym + x] +
+                                a[zc + yp + x] + a[zm + yc + x] + a[zp + yc + x]) / 7.0;
+            }
+          }
         }
       }
-  // 3 Jacobi passes: mean of self and the 6 face neighbours, periodic.
-  std::vector<double> T2(3 * n);
-  for (int pass = 0; pass < 3; ++pass) {
-    for (int k = 0; k < 3; ++k) {
-      const double* a = &Q[k * n];
-      double* b = &T2[k * n];
-      for (int z = 0; z < N; ++z)
-        for (int y = 0; y < N; ++y)
-          for (int x = 0; x < N; ++x) {
-            auto at = [&](int X, int Y, int Z) {
-              X = (X + N) % N; Y = (Y + N) % N; Z = (Z + N) % N;
-              return a[((size_t)Z * N + Y) * N + X];
-            };
-            b[((size_t)z * N + y) * N + x] = (at(x, y, z) + at(x - 1, y, z) + at(x + 1, y, z) + at(x, y - 1, z) +
-                                              at(x, y + 1, z) + at(x, y, z - 1) + at(x, y, z + 1)) / 7.0;
-          }
-    }
-    Q.swap(T2);
+    });
+    std::swap(Q, T2);
   }
-  for (size_t i = 0; i < n; ++i)
-    for (int k = 0; k < 3; ++k) P[k * n + i] = phi[i] > 0.5 ? Q[k * n + i] : 0.0;
+  slabs([&](int z0, int z1) {
+    for (size_t i = (size_t)z0 * NN; i < (size_t)z1 * NN; ++i)
+      for (int k = 0; k < 3; ++k) P[k * n + i] = phi[i] > 0.5 ? Q[k * n + i] : 0.0;
+  });
   return TTSH_OK;
 }
