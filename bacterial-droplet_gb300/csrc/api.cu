@@ -1445,21 +1445,51 @@ int ttsh_run_dirs(const char* const* dirs, int n, const ttsh_ext* ext, uint64_t 
     bool active;
   };
   std::vector<Run> run(n);
-  for (int i = 0; i < n; ++i) {
-    const ttsh_input& p = in[i];
-    const size_t nn = (size_t)p.Nx * p.Nx * p.Nx;
-    std::vector<double> phi(nn), P(3 * nn), u(3 * nn), us(3 * nn), Ps(3 * nn);
-    const int t0 = (int)((p.T0 + 0.1 * p.dte) / p.dte);  // TTSH3D.cu:768
-    const std::string conf0 = std::string(dirs[i]) + "/../data/conf_" + std::to_string(t0) + ".dat";
-    rc = ttsh_init_reference(&p, (unsigned)(seed + (uint64_t)i), conf0.c_str(), phi.data(), P.data(), u.data(),
-                             us.data(), Ps.data());
-    if (!rc) rc = ttsh_set_state(s, i, phi.data(), P.data(), u.data(), us.data(), Ps.data());
-    if (!rc && p.T0 == 0) rc = ttsh_write_conf(s, i, (std::string(dirs[i]) + "/conf_0.dat").c_str());
+  // The initial states (the reference's generator, sequential within a droplet) are computed for
+  // several droplets at once on host threads, as many as fit in about 4 GiB of host arrays (13 N^3
+  // doubles each), then uploaded and written in directory order.
+  struct Init {
+    std::vector<double> phi, P, u, us, Ps;
+    int rc = 0;
+    std::string msg;
+  };
+  size_t per = 0;
+  for (int i = 0; i < n; ++i) per = std::max(per, 13 * (size_t)in[i].Nx * in[i].Nx * in[i].Nx * sizeof(double));
+  const int conc = (int)std::max<size_t>(
+      1, std::min<size_t>(std::max(1u, std::thread::hardware_concurrency()), ((size_t)4 << 30) / std::max<size_t>(per, 1)));
+  for (int b = 0; b < n; b += conc) {
+    const int e = std::min(n, b + conc);
+    std::vector<Init> ini(e - b);
+    std::vector<std::thread> th;
+    for (int i = b; i < e; ++i)
+      th.emplace_back([&, i]() {
+        const ttsh_input& p = in[i];
+        const size_t nn = (size_t)p.Nx * p.Nx * p.Nx;
+        Init& w = ini[i - b];
+        w.phi.resize(nn);
+        w.P.resize(3 * nn);
+        w.u.resize(3 * nn);
+        w.us.resize(3 * nn);
+        w.Ps.resize(3 * nn);
+        const int t0 = (int)((p.T0 + 0.1 * p.dte) / p.dte);  // TTSH3D.cu:768
+        const std::string conf0 = std::string(dirs[i]) + "/../data/conf_" + std::to_string(t0) + ".dat";
+        w.rc = ttsh_init_reference(&p, (unsigned)(seed + (uint64_t)i), conf0.c_str(), w.phi.data(), w.P.data(),
+                                   w.u.data(), w.us.data(), w.Ps.data());
+        if (w.rc) w.msg = ttsh_last_error();  // the error text is per thread
+      });
+    for (auto& t : th) t.join();
+    for (int i = b; i < e && !rc; ++i) {
+      const ttsh_input& p = in[i];
+      Init& w = ini[i - b];
+      rc = w.rc ? set_error(w.rc, w.msg) : 0;
+      if (!rc) rc = ttsh_set_state(s, i, w.phi.data(), w.P.data(), w.u.data(), w.us.data(), w.Ps.data());
+      if (!rc && p.T0 == 0) rc = ttsh_write_conf(s, i, (std::string(dirs[i]) + "/conf_0.dat").c_str());
+      run[i] = {p.T0, p.dt0, p.dte, p.Ts, true};
+    }
     if (rc) {
       ttsh_destroy(s);
       return rc;
     }
-    run[i] = {p.T0, p.dt0, p.dte, p.Ts, true};
   }
   // opt-in autotuning (TTSH_TUNE=1; TTSH_TUNE_CACHE names a cache file), on the initial fields
   if (const char* tv = std::getenv("TTSH_TUNE")) {
