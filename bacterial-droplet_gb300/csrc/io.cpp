@@ -203,33 +203,77 @@ int ttsh_init_reference(const ttsh_input* in, unsigned seed, const char* conf0_p
   const int N = in->Nx;
   if (N <= 0 || in->Ny != N || in->Nz != N) return set_error(TTSH_E_INVALID, "ttsh_init_reference: grid");
   const size_t n = (size_t)N * N * N;
-  std::fill(phi, phi + n, 0.0);
-  std::fill(P, P + 3 * n, 0.0);
-  std::fill(u, u + 3 * n, 0.0);
-  std::fill(ustar, ustar + 3 * n, 0.0);
-  std::fill(Pstar, Pstar + 3 * n, 0.0);
-  std::default_random_engine rng(seed);
-  std::uniform_real_distribution<double> randUR;
-  std::ifstream conf;
-  if (in->InitCond == 0 && conf0_path) conf.open(conf0_path);
-  for (int i = 0; i < N; i++)
-    for (int j = 0; j < N; j++)
-      for (int k = 0; k < N; k++) {
-        const size_t idx = ((size_t)k * N + j) * N + i;  // x = i, y = j, z = k (TTSH3D.cu:786-791)
-        if (in->InitCond == 0) {
+  if (in->InitCond != 1) {
+    std::fill(phi, phi + n, 0.0);
+    std::fill(P, P + 3 * n, 0.0);
+    std::fill(u, u + 3 * n, 0.0);
+    std::fill(ustar, ustar + 3 * n, 0.0);
+    std::fill(Pstar, Pstar + 3 * n, 0.0);
+  }
+  if (in->InitCond == 0) {  // the two velocity columns of data/conf_<t0>.dat, in the same loop order
+    std::ifstream conf;
+    if (conf0_path) conf.open(conf0_path);
+    for (int i = 0; i < N; i++)
+      for (int j = 0; j < N; j++)
+        for (int k = 0; k < N; k++) {
+          const size_t idx = ((size_t)k * N + j) * N + i;  // x = i, y = j, z = k (TTSH3D.cu:786-791)
           conf >> u[idx] >> u[n + idx];
-        } else if (in->InitCond == 1) {
-          double* tgt[12] = {&u[idx], &u[n + idx], &u[2 * n + idx], &ustar[idx], &ustar[n + idx],
-                             &ustar[2 * n + idx], &P[idx], &P[n + idx], &P[2 * n + idx], &Pstar[idx],
-                             &Pstar[n + idx], &Pstar[2 * n + idx]};
-          for (int c = 0; c < 12; ++c) *tgt[c] = 0 + in->init0 * (randUR(rng) - 0.5);
-          const double dx = (i - in->Nx / 2.), dy = (j - in->Ny / 2.), dz = (k - in->Nz / 2.);
-          const double r = std::sqrt(dx * dx + dy * dy + dz * dz);
-          phi[idx] = (1 - std::tanh((r - in->Nx / 4.) * 2)) / 2;
-          (void)randUR(rng);  // p_v (recomputed by the first projection)
-          (void)randUR(rng);  // p_p
         }
+    return TTSH_OK;
+  }
+  if (in->InitCond != 1) return TTSH_OK;
+  // InitCond 1: 14 draws per site (12 fields, then p_v and p_p, which the first projection
+  // recomputes) in the loop order x, y, z (z innermost), from std::default_random_engine(seed)
+  // through uniform_real_distribution<double>. That engine is minstd_rand0 (x <- 16807 x mod
+  // 2^31 - 1), and each double draw takes two of its outputs (generate_canonical<double, 53> of a
+  // 2^31 - 2 wide range), so site s starts at the state x_0 16807^(28 s): the sites are drawn on
+  // all host cores with the reference's numbers.
+  constexpr uint64_t LCG_A = 16807, LCG_M = 2147483647;
+  auto powmod = [](uint64_t b, uint64_t e) {
+    uint64_t r = 1;
+    for (b %= LCG_M; e; e >>= 1, b = b * b % LCG_M)
+      if (e & 1) r = r * b % LCG_M;
+    return r;
+  };
+  const uint64_t x0 = (uint64_t)seed % LCG_M == 0 ? 1 : (uint64_t)seed % LCG_M;  // the engine's seeding rule
+  // Work unit: XB consecutive x = i (one 64-byte line of each field along x), one engine per x
+  // column started at its first site s = i N^2, the sites then visited in (y, z, x) order so that
+  // the writes fill whole lines; units go to the threads round-robin.
+  constexpr int XB = 8;
+  const int nunits = (N + XB - 1) / XB;
+  const unsigned nth = std::max(1u, std::min({64u, std::thread::hardware_concurrency(), (unsigned)nunits}));
+  const uint64_t step_col = powmod(LCG_A, 28 * (uint64_t)N * N);  // one x column: N^2 sites
+  const uint64_t start0 = x0;
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < nth; ++t)
+    th.emplace_back([&, t]() {
+      for (int unit = (int)t; unit < nunits; unit += (int)nth) {
+        const int ia = unit * XB, nb = std::min(XB, N - ia);
+        std::default_random_engine rng[XB];
+        uint64_t st = start0 * powmod(step_col, (uint64_t)ia) % LCG_M;  // state at site s = ia N^2
+        for (int b = 0; b < nb; ++b) {
+          rng[b].seed((std::default_random_engine::result_type)st);
+          st = st * step_col % LCG_M;
+        }
+        std::uniform_real_distribution<double> randUR;
+        for (int j = 0; j < N; j++)
+          for (int k = 0; k < N; k++)
+            for (int b = 0; b < nb; ++b) {
+              const int i = ia + b;
+              const size_t idx = ((size_t)k * N + j) * N + i;  // x = i, y = j, z = k (TTSH3D.cu:786-791)
+              double* tgt[12] = {&u[idx], &u[n + idx], &u[2 * n + idx], &ustar[idx], &ustar[n + idx],
+                                 &ustar[2 * n + idx], &P[idx], &P[n + idx], &P[2 * n + idx], &Pstar[idx],
+                                 &Pstar[n + idx], &Pstar[2 * n + idx]};
+              for (int c = 0; c < 12; ++c) *tgt[c] = 0 + in->init0 * (randUR(rng[b]) - 0.5);
+              const double dx = (i - in->Nx / 2.), dy = (j - in->Ny / 2.), dz = (k - in->Nz / 2.);
+              const double r = std::sqrt(dx * dx + dy * dy + dz * dz);
+              phi[idx] = (1 - std::tanh((r - in->Nx / 4.) * 2)) / 2;
+              (void)randUR(rng[b]);  // p_v (recomputed by the first projection)
+              (void)randUR(rng[b]);  // p_p
+            }
       }
+    });
+  for (auto& x : th) x.join();
   return TTSH_OK;
 }
 

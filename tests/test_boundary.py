@@ -281,3 +281,54 @@ def test_snapshot_number_format_on_hard_values(tmp_path):
     exp = "".join("%.15f %.15f " % (u[0, z, y, x], u[1, z, y, x])
                   for y in range(N) for x in range(N) for z in range(N))
     assert open(path2).read() == exp
+
+
+def _minstd_canonical_stream(seed, count):
+    """The reference's draws (TTSH3D.cu:40, :801-824): std::default_random_engine (libstdc++:
+    minstd_rand0, x <- 16807 x mod 2^31 - 1) through uniform_real_distribution<double>(0, 1), i.e.
+    generate_canonical<double, 53>: two engine outputs per draw, (x1 - 1) + (x2 - 1) r over r^2 with
+    r = 2^31 - 2, in double arithmetic."""
+    m, a = 2147483647, 16807
+    x = seed % m or 1
+    r = 2147483646.0
+    out = []
+    for _ in range(count):
+        x = x * a % m
+        s = float(x - 1) * 1.0
+        x = x * a % m
+        s = s + float(x - 1) * r
+        v = s / (r * r)
+        out.append(v if v < 1.0 else 0.9999999999999999)
+    return out
+
+
+def test_init_reference_draws_follow_the_reference_generator():
+    """ttsh_init_reference with InitCond 1 (the shim's and the sweep driver's initial state) against
+    a pure-Python restatement of the reference's generator: 14 draws per site in the reference's
+    loop order (x outer, z inner): u, u*, P, P* as init0 (draw - 1/2), then p_v and p_p."""
+    import numpy as np
+    import ttsh
+    N = 8
+    inp = ttsh.default_input(Nx=N, Ny=N, Nz=N)
+    for seed in (12345, 0, 2147483647, 4294967295):  # 0 and multiples of 2^31 - 1 seed the state 1
+        _check_reference_draws(np, ttsh, inp, N, seed)
+
+
+def _check_reference_draws(np, ttsh, inp, N, seed):
+    st = ttsh.init_reference(inp, seed)
+    d = _minstd_canonical_stream(seed, 14 * N ** 3)
+    init0 = inp.init0
+    k = 0
+    for i in range(N):
+        for j in range(N):
+            for z in range(N):
+                vals = [init0 * (d[k + c] - 0.5) for c in range(12)]
+                k += 14
+                got = [st["u"][0, z, j, i], st["u"][1, z, j, i], st["u"][2, z, j, i],
+                       st["us"][0, z, j, i], st["us"][1, z, j, i], st["us"][2, z, j, i],
+                       st["P"][0, z, j, i], st["P"][1, z, j, i], st["P"][2, z, j, i],
+                       st["ps"][0, z, j, i], st["ps"][1, z, j, i], st["ps"][2, z, j, i]]
+                assert got == vals, (i, j, z)
+                r = np.sqrt((i - N / 2) ** 2 + (j - N / 2) ** 2 + (z - N / 2) ** 2)
+                # (numpy's tanh and the C library's may differ in the last bit)
+                assert abs(st["phi"][z, j, i] - (1 - np.tanh((r - N / 4) * 2)) / 2) <= 1e-15
